@@ -1,0 +1,129 @@
+/*
+ * rr_oracle.h -- CPU restatement (FP64, plain C) of the reference's
+ * recursively-regularized lattice-Boltzmann time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * the smoke check and the CPU-baseline leg of the benchmark call it.  The
+ * product path (the CUDA library behind include/rr_api.h) never links,
+ * loads or calls anything in this directory.
+ *
+ * Every routine follows one reference routine operation by operation (same
+ * association of sums and products, same loop order), so that with
+ * -ffp-contract=off the results are reproducible bit for bit on any IEEE
+ * host.  Citations are path:line inside the reference project.
+ *
+ * Pinning: the restatement is checked against
+ *   - the Taylor-Green golden midline Taylor_Green/RRBMa0.01L100.txt:3-102,
+ *   - the reference CUDA channel kernels compiled for the host from their own
+ *     sources (oracle/ref_build.sh -> oracle/_ref/), bit for bit.
+ */
+#ifndef RR_ORACLE_H
+#define RR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* velocity orderings */
+#define ORC_ORDER_CUDA 0    /* RR27V33_code_DNS_LES/initial.cu:67-69 */
+#define ORC_ORDER_FORTRAN 1 /* Taylor_Green/D3Q27RR.f90:69-71, Cavity/para.f90:126-128 */
+
+/* definition of the lattice sound speed */
+#define ORC_CS_SQRT_RT 0   /* cs = sqrt(1/3): initial.cu:79-80, Cavity/para.f90:98 */
+#define ORC_CS_INV_SQRT3 1 /* cs = 1/sqrt(3): Taylor_Green/D3Q27RR.f90:27 */
+
+/* face kinds, faces ordered x-lo, x-hi, y-lo, y-hi, z-lo, z-hi */
+#define ORC_FACE_PERIODIC 0
+#define ORC_FACE_WALL 1    /* half-way bounce-back + regularized closure */
+#define ORC_FACE_WALL_BB 2 /* half-way bounce-back only */
+
+typedef struct {
+    int q;   /* 19 or 27 */
+    int ord; /* ORC_ORDER_* */
+    int cx[27], cy[27], cz[27], opp[27];
+    double w[27];
+    double rt, cs, cs3;
+    double H100[27], H010[27], H001[27];
+    double H110[27], H101[27], H011[27], H200[27], H020[27], H002[27];
+    double H210[27], H201[27], H021[27], H120[27], H102[27], H012[27], H111[27];
+    /* D3Q19 admissible third-order combinations (Taylor_Green/D3Q19RR.f90:131-136) */
+    double Hp1[27], Hm1[27], Hp2[27], Hm2[27], Hp3[27], Hm3[27];
+} orc_lattice;
+
+typedef struct {
+    int nx, ny, nz;
+    orc_lattice lat;
+    double tau;
+    double force[3]; /* uniform body force */
+    int les;         /* WALE eddy viscosity on/off */
+    double cw;       /* WALE constant */
+    int face[6];     /* ORC_FACE_* */
+    double uwall[6][3];
+    /* Taylor_Green/D3Q27RR.f90 and D3Q19RR.f90 declare their Hermite tables and
+     * intermediates as default REAL (D3Q27RR.f90:45-61): with this flag the
+     * collision and the start state round them to single precision as that
+     * program does; populations, moments and weights stay REAL(8). */
+    int tg_real4;
+} orc_params;
+
+/* State in the reference's own form: populations after streaming and wall
+ * treatment, the macroscopic fields computed from them, and the eddy
+ * viscosity of the last collision.  SoA, f[ip*N + (z*ny + y)*nx + x]. */
+typedef struct {
+    double *f, *ftmp;
+    double *rho, *ux, *uy, *uz, *taut;
+} orc_state;
+
+int orc_lattice_init(orc_lattice *L, int q, int order, int cs_mode);
+
+double orc_feq(const orc_lattice *L, int ip, double rho9, double u9, double v9, double w9);
+
+void orc_collide_node(const orc_lattice *L, double tau_eff, const double F[3], double rho9,
+                      double u9, double v9, double w9, double *f);
+
+void orc_regularize_node(const orc_lattice *L, const double F[3], double *f,
+                         const int *entering);
+
+void orc_moments_node(const orc_lattice *L, const double F[3], const double *f, double *rho,
+                      double *u, double *v, double *w);
+
+/* one full reference time step on the whole grid */
+void orc_step(const orc_params *P, orc_state *S);
+void orc_run(const orc_params *P, orc_state *S, int nsteps);
+
+/* WALE eddy viscosity (LES.cu:4-98), generalised to walls on any face */
+void orc_wale(const orc_params *P, const double *ux, const double *uy, const double *uz,
+              double *taut);
+
+/* the streaming + wall part of a step, on its own: fin (post-collision) ->
+ * fout (post-stream, walls applied); used to check the product's f readout */
+void orc_stream_walls(const orc_params *P, const double *fin, double *fout);
+void orc_moments_all(const orc_params *P, const double *f, double *rho, double *ux, double *uy,
+                     double *uz);
+void orc_collide_all(const orc_params *P, double *f, const double *rho, const double *ux,
+                     const double *uy, const double *uz, const double *taut);
+
+/* initial states */
+void orc_init_tg_reference(const orc_params *P, double U0, double *f, double *rho, double *ux,
+                           double *uy, double *uz);
+void orc_init_tg_config(const orc_params *P, double U0, double *f, double *rho, double *ux,
+                        double *uy, double *uz);
+void orc_init_equilibrium2(const orc_params *P, double *f, const double *rho, const double *ux,
+                           const double *uy, const double *uz);
+void orc_init_channel_loglaw(const orc_params *P, double ustar, double ystar, double *f,
+                             double *rho, double *ux, double *uy, double *uz);
+
+/* counter-based random numbers shared with the CUDA library (splitmix64) */
+uint64_t orc_splitmix64(uint64_t x);
+double orc_uniform_pm1(uint64_t seed, uint64_t node, uint64_t comp);
+void orc_init_channel_config(const orc_params *P, double uc, double amp, uint64_t seed,
+                             double *f, double *rho, double *ux, double *uy, double *uz);
+
+void orc_set_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
