@@ -1,0 +1,314 @@
+"""Benchmark: D3Q27 RR lattice updates per second on one GB300.
+
+Workload (the configuration the headline metric is quoted on): lid-driven
+cavity, 128^3, D3Q27 RR, Re = 1000, lid 0.1 in +x on the top (y-hi) wall,
+half-way bounce-back on all six faces, FP16 shifted-population storage with
+FP32 arithmetic.  One "step" = one fused time step over the whole grid.
+
+Line fields (one JSON line on rank 0):
+  value      MLUPS over the timed steps, each step timed alone with CUDA
+             events on the solver's stream, L2 flushed (256 MB write) before
+             every timed step; inputs resident in HBM.
+  e2e        the same metric through the C ABI with host buffers: upload of
+             the start state from pinned host memory (rr_init_state), the K
+             steps, and the macroscopic fields read back to the host
+             (rr_macro), all inside the timed region.
+  roofline   the step kernel against the measured HBM copy bandwidth:
+             algorithmic bytes = 27 populations x 2 B read + written = 108 B
+             per lattice update.
+  cpu_baseline  the oracle (C restatement of the reference step, OpenMP on
+             all host threads) on a bounded sample of the same workload.
+--impl reference runs that CPU implementation alone as the reference arm.
+Multi-GPU (torchrun, N > 1): independent replicas, one domain per GPU.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "recursively-regularized-lbm_gb300"))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "cavity128_f16": dict(kind="cavity", n=128, storage="f16", Re=1000.0, U=0.1),
+    "cavity128_f32": dict(kind="cavity", n=128, storage="f32", Re=1000.0, U=0.1),
+    "cavity128_f64": dict(kind="cavity", n=128, storage="f64", Re=1000.0, U=0.1),
+    "cavity128_bf16": dict(kind="cavity", n=128, storage="bf16", Re=1000.0, U=0.1),
+    "channel_les_f16": dict(kind="channel", storage="f16"),
+    "tg100_f64": dict(kind="tg", storage="f64"),
+}
+BYTES_PER_POP = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}
+DTYPE = {"f64": "f64", "f32": "f32", "f16": "f16-store/f32-compute", "bf16": "bf16-store/f32-compute"}
+
+
+def make(wl):
+    from rrlbm import presets
+    w = WORKLOADS[wl]
+    if w["kind"] == "cavity":
+        return presets.cavity(n=w["n"], Re=w["Re"], U=w["U"], storage=w["storage"], variant="config")
+    if w["kind"] == "channel":
+        return presets.channel(storage=w["storage"], les=True, variant="config")
+    return presets.taylor_green(L=100, nz=4, tau=0.6, Ma=0.01, storage=w["storage"])
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic(wl):
+    """DRAM bytes per step-kernel launch from the committed ncu summary, if any"""
+    path = os.path.join(ROOT, "profiles", f"step_kernel_{wl}.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region"""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap,utilization.gpu")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return None
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                util = float(s[7])
+                if util > 0:
+                    sm.append(float(s[0]))
+                mx = max(mx, float(s[1]))
+                for k, v in zip(names, s[3:7]):
+                    if v.lower() == "active":
+                        reasons.add(k)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def cpu_baseline(wl, budget_s):
+    """the oracle on the machine's host cores, on whole steps of the workload"""
+    from oracle import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import load_state, oracle_for
+    p, st = make(wl)
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    o = oracle_for(p)
+    load_state(o, st)
+    o.run(1)  # warm
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.run(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s:
+            break
+    mlups = p.n * steps / el / 1e6
+    return {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{steps} full steps of the {p.lx}x{p.ly}x{p.lz} workload in FP64 "
+                      f"({el:.1f} s), OpenMP over {cores} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    K, W = args.steps, args.warmup
+    from oracle import oracle as O
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import load_state, oracle_for
+    p, st = make(args.workload)
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    o = oracle_for(p)
+    load_state(o, st)
+    o.run(W)
+    t0 = time.perf_counter()
+    o.run(K)
+    el = time.perf_counter() - t0
+    v = p.n * K / el / 1e6
+    line = {"metric": "D3Q27 RR MLUPS (lattice updates per second)", "value": v, "unit": "MLUPS",
+            "impl": "reference", "n_gpus": args.gpus, "steps": K, "warmup": W,
+            "ms_per_step": el / K * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"lid-driven cavity {p.lx}^3 D3Q27 RR Re=1000 (oracle: C "
+                                   "restatement of Cavity/*.f90 extended to six walls)"},
+            "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
+                             "sample": f"{K} full steps after {W} warm-up steps, OpenMP over {cores} threads"},
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import rrlbm
+
+    K, W = args.steps, args.warmup
+    torch.cuda.set_device(local_rank)
+    p, st = make(args.workload)
+    p.device = local_rank
+    storage = WORKLOADS[args.workload]["storage"]
+    q = p.q
+    n = p.n
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    s = rrlbm.Solver(p)
+    s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
+    stream = torch.cuda.ExternalStream(s.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # warm-up (also builds nothing lazily on the timed path)
+    s.step(W)
+    s.sync()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local_rank) as clk:
+        for k in range(K):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))  # evict the populations from L2
+                evs[k][0].record(stream)
+            s.step(1)
+            with torch.cuda.stream(stream):
+                evs[k][1].record(stream)
+        s.sync()
+        torch.cuda.synchronize()
+    times = [a.elapsed_time(b) for a, b in evs]  # ms
+    t_step = sum(times) / K
+    if dist:
+        t = torch.tensor([t_step], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = n * world / (t_step * 1e-3) / 1e6
+
+    # end to end through the C ABI with host buffers
+    pin = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in ("rho", "ux", "uy", "uz")}
+    outs = {k: torch.empty((n,), dtype=torch.float64).pin_memory() for k in ("rho", "ux", "uy", "uz")}
+    s2 = rrlbm.Solver(p)
+    arr = {k: pin[k].numpy() for k in pin}
+    s2.init_state(arr["rho"], arr["ux"], arr["uy"], arr["uz"])
+    s2.step(W)
+    s2.sync()
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s2.init_state(arr["rho"], arr["ux"], arr["uy"], arr["uz"])
+    s2.step(K)
+    s2.macro_into(*(outs[k].numpy().reshape(p.shape) for k in ("rho", "ux", "uy", "uz")))
+    e2e_t = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_t], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e = n * K * world / e2e_t / 1e6
+    assert np.isfinite(outs["ux"].numpy()).all()
+    s2.close()
+    s.close()
+    if rank != 0:
+        return
+    pk, src = peaks()
+    bpl = 2 * q * BYTES_PER_POP[storage]
+    achieved = n * bpl / (t_step * 1e-3) / 1e9
+    traffic = ncu_traffic(args.workload)
+    line = {
+        "metric": "D3Q27 RR MLUPS (lattice updates per second)", "value": value, "unit": "MLUPS",
+        "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": t_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[storage], "data": "synthetic",
+        "config": {"workload": f"lid-driven cavity {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Re=1000, lid 0.1 +x "
+                               f"on y-hi, bounce-back + regularized closure on 6 faces, {storage} storage",
+                   "nodes": n, "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed (256 MB write) before every timed step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "bytes_per_lup": bpl, "peak_source": f"{src} (hbm_gbs)"},
+        "e2e": {"value": e2e, "unit": "MLUPS", "h2d_bytes_per_step": 4 * 8 * n / K,
+                "d2h_bytes_per_step": 4 * 8 * n / K,
+                "what": "rr_init_state from pinned host arrays + K steps + rr_macro to pinned host arrays"},
+        "gpu_launches": K,
+        "clocks": clk.summary(),
+        "step_ms_min": min(times), "step_ms_max": max(times),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cavity128_f16", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    try:
+        run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+/*
+ * rr_api.h -- C ABI of the GB300 recursively-regularized lattice-Boltzmann
+ * solver (librrlbm.so).  Plain pointers and sizes only.
+ *
+ * It replaces the host loop of the reference CUDA channel code,
+ * RR27V33_code_DNS_LES/main.cu:31-117, whose body calls the kernels declared
+ * in RR27V33_code_DNS_LES/LBMLES.h:60-81 on global device arrays and then the
+ * output routines of LBMLES.h:83-86.  With this library that loop becomes
+ *
+ *     rr_params p; rr_params_default(&p);  ... set knobs ...
+ *     rr_solver *s; rr_create(&p, &s);
+ *     rr_init_state(s, f, rho, ux, uy, uz, RR_HOST);      // initialize()
+ *     for (istep = 1; istep <= NEND; istep++) {
+ *         rr_step(s, 1);                                  // main.cu:360-409
+ *         if (istep % NDIAG == 0) rr_output(s, RR_OUT_DIAG, "data");
+ *         ...
+ *     }
+ *     rr_destroy(s);
+ *
+ * Every function returns an rr_status and never exits the process; the text
+ * of the last error of the calling thread is available from rr_last_error().
+ * All device work of a solver runs on that solver's own CUDA stream;
+ * rr_step() only enqueues work, rr_sync() waits for it and reports the
+ * device-side watchdog (density out of range or NaN).
+ */
+#ifndef RR_API_H
+#define RR_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    RR_OK = 0,
+    RR_ERR_INVALID = 1,     /* bad argument or parameter */
+    RR_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    RR_ERR_NOMEM = 3,       /* device or host allocation failed */
+    RR_ERR_UNSUPPORTED = 4, /* combination not built */
+    RR_ERR_WATCHDOG = 5,    /* density left (0.1, 10) or became NaN */
+    RR_ERR_IO = 6,          /* file could not be opened / read / written */
+    RR_ERR_STATE = 7        /* call out of order (e.g. step before init) */
+} rr_status;
+
+/* population storage in HBM; arithmetic is FP64 for RR_STORE_F64, FP32 else */
+typedef enum { RR_STORE_F64 = 0, RR_STORE_F32 = 1, RR_STORE_F16 = 2, RR_STORE_BF16 = 3 } rr_storage;
+
+/* face kinds; faces are ordered x-lo, x-hi, y-lo, y-hi, z-lo, z-hi */
+typedef enum {
+    RR_FACE_PERIODIC = 0,
+    RR_FACE_WALL = 1,    /* half-way bounce-back + regularized closure (RRBC) */
+    RR_FACE_WALL_BB = 2  /* half-way bounce-back only */
+} rr_face;
+
+/* velocity ordering of populations crossing the API (rr_init_state, rr_get_f,
+ * rr_save / rr_load):  RR_ORDER_CUDA = RR27V33_code_DNS_LES/initial.cu:67-69,
+ * RR_ORDER_FORTRAN = Taylor_Green/D3Q27RR.f90:69-71 = Cavity/para.f90:126-128
+ * (the only ordering defined for D3Q19, Taylor_Green/D3Q19RR.f90:75-77) */
+typedef enum { RR_ORDER_CUDA = 0, RR_ORDER_FORTRAN = 1 } rr_order;
+
+/* where a caller buffer lives */
+typedef enum { RR_HOST = 0, RR_DEVICE = 1 } rr_where;
+
+/* rr_output() selectors: the reference's four outputs (output.cu) */
+#define RR_OUT_DIAG 1u    /* diag_flow: console line + data/statistics.dat (output.cu:3-66) */
+#define RR_OUT_FLOW 2u    /* output_flow: data/%09d.dat rho,ux,uy,uz FP64 (output.cu:68-140) */
+#define RR_OUT_PROFILE 4u /* output_profile: data/Profiles.txt (output.cu:142-225) */
+#define RR_OUT_F 8u       /* output_f: data/f%09d.dat, 27 N FP64 (output.cu:227-258) */
+
+/* Run-time counterpart of parameters.h:1-25 and globals.cu:18-40. */
+typedef struct rr_params {
+    int lx, ly, lz;      /* LX, LY, LZ (parameters.h:9-11) */
+    int q;               /* NPOP: 27, or 19 (Taylor_Green/D3Q19RR.f90) */
+    int use_les;         /* USE_LES (parameters.h:6): WALE eddy viscosity */
+    double tau;          /* relaxation time, tau = 3 nu + 0.5 (globals.cu:36) */
+    double cw;           /* WALE constant (LES.cu:12) */
+    double force[3];     /* uniform body force; force_in_x = 2 u*^2 / LY (globals.cu:38) */
+    int face[6];         /* rr_face of x-lo, x-hi, y-lo, y-hi, z-lo, z-hi */
+    double uwall[6][3];  /* velocity of each wall face (moving lid, Cavity/streaming.f90:142-152) */
+    int storage;         /* rr_storage */
+    int order;           /* rr_order of populations crossing the API */
+    int device;          /* CUDA device ordinal */
+    double ustar, ystar; /* friction velocity and viscous length, for output_profile's y+ */
+} rr_params;
+
+typedef struct rr_solver rr_solver;
+
+/* The defaults of parameters.h / globals.cu: 64^3 Re_tau = 180 channel, DNS,
+ * walls at y = 0 and y = LY-1, periodic x and z, nu = 0.000622,
+ * u* = 2 Re_tau nu / LY, tau = 3 nu + 0.5, F_x = 2 u*^2 / LY, D3Q27, FP64. */
+rr_status rr_params_default(rr_params *p);
+
+/* allocation of device state: initialize() (initial.cu:4-19) */
+rr_status rr_create(const rr_params *p, rr_solver **out);
+rr_status rr_destroy(rr_solver *s);
+
+/* Sets the state the reference holds before its first step: post-stream
+ * populations f (NPOP x N FP64, f[ip * N + (z * LY + y) * LX + x], in
+ * p->order) and the macroscopic fields the first collision uses
+ * (init_arrays, initial.cu:268-326, and the CONTINUE_STEP restart,
+ * initial.cu:189-265).  f may be NULL: the second-order equilibrium of
+ * (rho, u) is used (Cavity/initial.f90:3-34).  Resets the step counter. */
+rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const double *ux,
+                        const double *uy, const double *uz, int where);
+
+/* nsteps full time steps (main.cu:360-409), one fused kernel each, enqueued
+ * on the solver's stream (CUDA graphs for long runs). */
+rr_status rr_step(rr_solver *s, int nsteps);
+rr_status rr_sync(rr_solver *s);
+long long rr_get_istep(const rr_solver *s);
+/* the solver's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or CUDA events against the solver's; no counterpart in the reference,
+ * which runs everything on the default stream (main.cu:381-409) */
+void *rr_get_stream(const rr_solver *s);
+
+/* Macroscopic fields after the last step, what the reference holds in
+ * d_rho, d_ux, d_uy, d_uz (FP64, N each).  taut (may be NULL) receives the
+ * WALE eddy viscosity tau_t = 3 nu_t of those fields, i.e. the one the next
+ * collision uses.  Any pointer may be NULL. */
+rr_status rr_macro(rr_solver *s, double *rho, double *ux, double *uy, double *uz, double *taut,
+                   int where);
+
+/* Post-stream populations after the last step (d_f after main.cu:64 and the
+ * wall closure), FP64, NPOP x N, in p->order. */
+rr_status rr_get_f(rr_solver *s, double *f, int where);
+
+/* diag_flow's statistics (output.cu:24-35): {umean, vmean, wmean, rhomean} */
+rr_status rr_diag(rr_solver *s, double out[4]);
+
+/* output_profile's statistics per y plane (output.cu:181-214), FP64 on the
+ * device: out[iy * 11 + k] for k = y+0.5, (y+0.5)/ystar, <u>, <v>, <w>,
+ * <u'u'>, <v'v'>, <w'w'>, <u'v'>, <u'w'>, <v'w'>, and out[LY*11 + iy] = <tau_t>
+ * (out must hold 12 * LY doubles). */
+rr_status rr_profile(rr_solver *s, double *out);
+
+/* Time-averaging accumulators (FP64, on the device): rr_accumulate() adds the
+ * current y-plane profile (12 * LY values, as rr_profile) to the running sums;
+ * rr_get_accum() returns the sums and the number of samples. */
+rr_status rr_accumulate(rr_solver *s);
+rr_status rr_get_accum(rr_solver *s, double *sums, long long *samples);
+
+/* The reference's file outputs, byte-compatible (what = RR_OUT_* bits),
+ * written under directory dir with istep = rr_get_istep(). */
+rr_status rr_output(rr_solver *s, unsigned what, const char *dir);
+
+/* Restart files in the reference's format (output_flow + output_f, read
+ * back by initialize() with CONTINUE_STEP, initial.cu:189-265):
+ * dir/%09d.dat and dir/f%09d.dat. */
+rr_status rr_save(rr_solver *s, const char *dir);
+rr_status rr_load(rr_solver *s, const char *dir, long long istep);
+
+/* memory the solver holds on the device, in bytes */
+size_t rr_device_bytes(const rr_solver *s);
+/* bytes a solver with these parameters would hold (admission control) */
+size_t rr_bytes_for(const rr_params *p);
+
+/* text of the last error on this thread ("" if none) */
+const char *rr_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,593 @@
+// rr_api.cu -- host side of the C ABI declared in include/rr_api.h.
+//
+// A solver owns two population buffers (ping-pong), a CUDA stream, a watchdog
+// word and, lazily, FP64 scratch for readouts and statistics.  rr_step()
+// enqueues fused step kernels (CUDA graphs of GRAPH_STEPS steps for long
+// runs); nothing synchronises until a readout or rr_sync().
+#include <cuda_runtime.h>
+
+#include <cerrno>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/rr_api.h"
+#include "rr_aux.h"
+#include "rr_dispatch.h"
+#include "rr_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+rr_status fail(rr_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define RR_CK(call)                                                                            \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(RR_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),  \
+                        __FILE__, __LINE__);                                                   \
+    } while (0)
+
+constexpr int GRAPH_STEPS = 32; // steps per captured graph (even: ends on the same buffer)
+
+const rr::Ops &ops_for(int storage) {
+    switch (storage) {
+    case RR_STORE_F64: return rr::ops_f64();
+    case RR_STORE_F32: return rr::ops_f32();
+    case RR_STORE_F16: return rr::ops_f16();
+    default: return rr::ops_bf16();
+    }
+}
+
+unsigned long long padded_stride(uint32_t n) { return ((unsigned long long)n + 63ull) & ~63ull; }
+
+bool has_force(const rr_params &p) { return p.force[0] != 0.0 || p.force[1] != 0.0 || p.force[2] != 0.0; }
+
+rr_status validate(const rr_params *p) {
+    if (!p) return fail(RR_ERR_INVALID, "params is NULL");
+    if (p->lx < 1 || p->ly < 1 || p->lz < 1)
+        return fail(RR_ERR_INVALID, "grid %dx%dx%d must be positive", p->lx, p->ly, p->lz);
+    const double n = (double)p->lx * p->ly * p->lz;
+    if (n > 2147483647.0) return fail(RR_ERR_INVALID, "grid has %.0f nodes, limit 2^31-1", n);
+    if (p->q != 19 && p->q != 27) return fail(RR_ERR_INVALID, "q = %d, must be 19 or 27", p->q);
+    if (p->storage < RR_STORE_F64 || p->storage > RR_STORE_BF16)
+        return fail(RR_ERR_INVALID, "storage = %d unknown", p->storage);
+    if (!(p->tau > 0.5)) return fail(RR_ERR_INVALID, "tau = %g must exceed 0.5", p->tau);
+    if (p->order != RR_ORDER_CUDA && p->order != RR_ORDER_FORTRAN)
+        return fail(RR_ERR_INVALID, "order = %d unknown", p->order);
+    if (p->q == 19 && p->order != RR_ORDER_FORTRAN)
+        return fail(RR_ERR_INVALID, "D3Q19 populations exist only in the Fortran ordering");
+    const int n3[3] = {p->lx, p->ly, p->lz};
+    for (int f = 0; f < 6; f++) {
+        if (p->face[f] < RR_FACE_PERIODIC || p->face[f] > RR_FACE_WALL_BB)
+            return fail(RR_ERR_INVALID, "face[%d] = %d unknown", f, p->face[f]);
+        if (p->face[f] != RR_FACE_PERIODIC && n3[f / 2] < 2)
+            return fail(RR_ERR_INVALID, "a wall on face %d needs at least 2 nodes across", f);
+        if (p->face[f] == RR_FACE_PERIODIC &&
+            (p->uwall[f][0] != 0.0 || p->uwall[f][1] != 0.0 || p->uwall[f][2] != 0.0))
+            return fail(RR_ERR_INVALID, "face %d is periodic but has a wall velocity", f);
+    }
+    if ((p->face[0] == RR_FACE_PERIODIC) != (p->face[1] == RR_FACE_PERIODIC) ||
+        (p->face[2] == RR_FACE_PERIODIC) != (p->face[3] == RR_FACE_PERIODIC) ||
+        (p->face[4] == RR_FACE_PERIODIC) != (p->face[5] == RR_FACE_PERIODIC))
+        return fail(RR_ERR_INVALID, "an axis must be periodic on both faces or on neither");
+    if (p->use_les && !(p->cw >= 0.0)) return fail(RR_ERR_INVALID, "cw = %g", p->cw);
+    return RR_OK;
+}
+
+} // namespace
+
+struct rr_solver {
+    rr_params p;
+    const rr::Ops *ops = nullptr;
+    rr::Geom g{};
+    cudaStream_t stream = nullptr;
+    void *buf[2] = {nullptr, nullptr};
+    int cur = 0; // buffer holding the latest post-collision state
+    long long istep = 0;
+    bool ready = false;
+    bool stepped = false; // a step ran since the state was set: the previous buffer is valid
+    int *status = nullptr;   // device watchdog word
+    int *pos = nullptr;      // device: internal population -> API population
+    double *aux = nullptr;   // device FP64: rho, ux, uy, uz, taut (5 N)
+    double *stat = nullptr;  // device FP64: diag partials + outputs + profile + accumulators
+    long long acc_samples = 0;
+    size_t bytes = 0;
+    rr::LesTile tile{32, 8, 16};
+    cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+std::vector<int> api_positions(const rr_params &p) {
+    // internal order: CUDA order for D3Q27, Fortran (= only) order for D3Q19
+    std::vector<int> pos(p.q);
+    for (int i = 0; i < p.q; i++) pos[i] = i;
+    if (p.q == 27 && p.order == RR_ORDER_FORTRAN)
+        for (int j = 0; j < 27; j++) pos[rr::FORTRAN_TO_CUDA_27[j]] = j;
+    return pos;
+}
+
+size_t stat_doubles(const rr_params &p) {
+    // diag partials, 4 outputs, profile (12 ly), accumulators (12 ly)
+    return 4 * (size_t)rr::DIAG_MAX_BLOCKS + 4 + 24 * (size_t)p.ly;
+}
+
+rr_status ensure_aux(rr_solver *s) {
+    if (s->aux) return RR_OK;
+    const size_t n = s->g.n;
+    if (cudaMalloc(&s->aux, 5 * n * sizeof(double)) != cudaSuccess) {
+        s->aux = nullptr;
+        cudaGetLastError();
+        return fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of readout scratch", 5 * n * sizeof(double));
+    }
+    s->bytes += 5 * n * sizeof(double);
+    return RR_OK;
+}
+
+rr_status set_device(const rr_solver *s) {
+    RR_CK(cudaSetDevice(s->p.device));
+    return RR_OK;
+}
+
+// rho, u (and taut) of the current state into aux
+rr_status readout_macros(rr_solver *s, bool want_taut) {
+    rr_status st = ensure_aux(s);
+    if (st != RR_OK) return st;
+    const size_t n = s->g.n;
+    double *rho = s->aux, *ux = rho + n, *uy = ux + n, *uz = uy + n, *tt = uz + n;
+    // the previous buffer holds the post-collision state the last step read
+    RR_CK(s->ops->readout(s->p.q, has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, nullptr, 0,
+                          s->pos, rho, ux, uy, uz, s->stream));
+    if (want_taut) RR_CK(rr::launch_wale(s->g, s->p.cw, ux, uy, uz, tt, s->stream));
+    return RR_OK;
+}
+
+rr_status copy_out(rr_solver *s, double *dst, const double *src, size_t count, int where) {
+    if (!dst) return RR_OK;
+    RR_CK(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                          where == RR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          s->stream));
+    return RR_OK;
+}
+
+rr_status launch_steps(rr_solver *s, int n) {
+    const bool force = has_force(s->p);
+    const double om1 = 1.0 - 1.0 / s->p.tau;
+    for (int k = 0; k < n; k++) {
+        const void *fin = s->buf[s->cur];
+        void *fout = s->buf[1 - s->cur];
+        if (s->p.use_les)
+            RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
+                                   s->status, s->tile, s->stream));
+        else
+            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->stream));
+        s->cur = 1 - s->cur;
+    }
+    return RR_OK;
+}
+
+rr_status build_graph(rr_solver *s) {
+    if (s->graph) return RR_OK;
+    // captured from buffer 0; GRAPH_STEPS is even, so it ends on buffer 0
+    const int saved = s->cur;
+    s->cur = 0;
+    cudaGraph_t graph;
+    RR_CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    rr_status st = launch_steps(s, GRAPH_STEPS);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+    s->cur = saved;
+    if (st != RR_OK) return st;
+    if (e != cudaSuccess) return fail(RR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        s->graph = nullptr;
+        return fail(RR_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    }
+    return RR_OK;
+}
+
+rr_status write_file(const std::string &path, const void *data, size_t bytes, const char *mode) {
+    FILE *fp = fopen(path.c_str(), mode);
+    if (!fp) return fail(RR_ERR_IO, "cannot open %s: %s", path.c_str(), strerror(errno));
+    size_t w = fwrite(data, 1, bytes, fp);
+    int e = fflush(fp);
+    fclose(fp);
+    if (w != bytes || e != 0) return fail(RR_ERR_IO, "short write to %s", path.c_str());
+    return RR_OK;
+}
+
+rr_status ensure_dir(const char *dir) {
+    struct stat sb;
+    if (stat(dir, &sb) == 0) return RR_OK;
+    if (mkdir(dir, 0700) != 0 && errno != EEXIST) return fail(RR_ERR_IO, "cannot create %s", dir);
+    return RR_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *rr_last_error(void) { return g_err.c_str(); }
+
+rr_status rr_params_default(rr_params *p) {
+    if (!p) return fail(RR_ERR_INVALID, "params is NULL");
+    memset(p, 0, sizeof(*p));
+    // parameters.h:9-11 and globals.cu:33-38
+    p->lx = p->ly = p->lz = 64;
+    p->q = 27;
+    p->use_les = 0;
+    const double Re = 180.0, visc = 0.000622;
+    const double u0 = 2.0 * Re * visc / p->ly;
+    p->tau = 3.0 * visc + 0.5;
+    p->cw = 0.5;
+    p->force[0] = 2.0 * u0 * u0 / p->ly;
+    p->face[2] = p->face[3] = RR_FACE_WALL;
+    p->storage = RR_STORE_F64;
+    p->order = RR_ORDER_CUDA;
+    p->device = 0;
+    p->ustar = u0;
+    p->ystar = visc / u0;
+    return RR_OK;
+}
+
+size_t rr_bytes_for(const rr_params *p) {
+    if (!p || validate(p) != RR_OK) return 0;
+    const uint32_t n = (uint32_t)p->lx * p->ly * p->lz;
+    const size_t elem = p->storage == RR_STORE_F64 ? 8 : p->storage == RR_STORE_F32 ? 4 : 2;
+    return 2 * (size_t)p->q * padded_stride(n) * elem + 256 + stat_doubles(*p) * sizeof(double);
+}
+
+rr_status rr_create(const rr_params *p, rr_solver **out) {
+    if (!out) return fail(RR_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    rr_status st = validate(p);
+    if (st != RR_OK) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(RR_ERR_CUDA, "no CUDA device");
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(RR_ERR_INVALID, "device %d of %d", p->device, ndev);
+    rr_solver *s = new rr_solver();
+    s->p = *p;
+    s->ops = &ops_for(p->storage);
+    rr::Geom &g = s->g;
+    g.nx = p->lx;
+    g.ny = p->ly;
+    g.nz = p->lz;
+    g.n = (uint32_t)p->lx * p->ly * p->lz;
+    g.stride = padded_stride(g.n);
+    g.wallmask = 0;
+    for (int f = 0; f < 6; f++) {
+        g.face[f] = p->face[f];
+        if (p->face[f] != RR_FACE_PERIODIC) g.wallmask |= 1u << f;
+        for (int a = 0; a < 3; a++) g.uw[f][a] = p->uwall[f][a];
+    }
+    auto cleanup = [&](rr_status code) {
+        rr_destroy(s);
+        return code;
+    };
+    if (set_device(s) != RR_OK) return cleanup(RR_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(RR_ERR_CUDA, "stream creation failed"));
+    const size_t bytes = (size_t)p->q * g.stride * s->ops->elem_bytes;
+    for (int b = 0; b < 2; b++) {
+        if (cudaMalloc(&s->buf[b], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            s->buf[b] = nullptr;
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of populations", bytes));
+        }
+        s->bytes += bytes;
+    }
+    // one 256-byte block: the watchdog word, then the 27-entry population order
+    if (cudaMalloc(&s->status, 256) != cudaSuccess || cudaMemset(s->status, 0, 256) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the watchdog word"));
+    }
+    s->pos = s->status + 4;
+    std::vector<int> pos = api_positions(*p);
+    if (cudaMemcpy(s->pos, pos.data(), pos.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return cleanup(fail(RR_ERR_CUDA, "cannot upload the population order"));
+    const size_t sd = stat_doubles(*p) * sizeof(double);
+    if (cudaMalloc(&s->stat, sd) != cudaSuccess || cudaMemset(s->stat, 0, sd) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
+    }
+    s->bytes += 256 + sd;
+    // LES tile by size class: full 32-wide rows when x allows, else 16
+    s->tile.tx = p->lx >= 32 ? 32 : 16;
+    s->tile.ty = 256 / s->tile.tx;
+    s->tile.zchunk = p->lz >= 64 ? 16 : (p->lz >= 16 ? 8 : p->lz);
+    *out = s;
+    return RR_OK;
+}
+
+rr_status rr_destroy(rr_solver *s) {
+    if (!s) return RR_OK;
+    cudaSetDevice(s->p.device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    cudaFree(s->buf[0]);
+    cudaFree(s->buf[1]);
+    cudaFree(s->status);
+    cudaFree(s->aux);
+    cudaFree(s->stat);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    cudaGetLastError();
+    delete s;
+    return RR_OK;
+}
+
+rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const double *ux,
+                        const double *uy, const double *uz, int where) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (!rho || !ux || !uy || !uz) return fail(RR_ERR_INVALID, "rho, ux, uy, uz are required");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    const size_t n = s->g.n;
+    const size_t nf = f ? (size_t)s->p.q * n : 0;
+    double *tmp = nullptr;
+    const size_t tmp_count = 5 * n + nf;
+    RR_CK(cudaMallocAsync(&tmp, tmp_count * sizeof(double), s->stream));
+    double *d_rho = tmp, *d_ux = tmp + n, *d_uy = d_ux + n, *d_uz = d_uy + n, *d_tt = d_uz + n;
+    double *d_f = f ? d_tt + n : nullptr;
+    const cudaMemcpyKind kind = where == RR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaError_t e = cudaSuccess;
+    const double *src[4] = {rho, ux, uy, uz};
+    double *dst[4] = {d_rho, d_ux, d_uy, d_uz};
+    for (int k = 0; k < 4 && e == cudaSuccess; k++)
+        e = cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), kind, s->stream);
+    if (e == cudaSuccess && f) e = cudaMemcpyAsync(d_f, f, nf * sizeof(double), kind, s->stream);
+    // the reference's first step computes tau_t from these macros (main.cu:375-379)
+    if (e == cudaSuccess && s->p.use_les) e = rr::launch_wale(s->g, s->p.cw, d_ux, d_uy, d_uz, d_tt, s->stream);
+    if (e == cudaSuccess)
+        e = s->ops->upload(s->p.q, has_force(s->p), s->buf[0], s->g, s->p.tau, s->p.force, d_f, n,
+                           s->pos, d_rho, d_ux, d_uy, d_uz, s->p.use_les ? d_tt : nullptr, s->stream);
+    cudaError_t e2 = cudaFreeAsync(tmp, s->stream);
+    if (e != cudaSuccess) return fail(RR_ERR_CUDA, "state upload failed: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(RR_ERR_CUDA, "cudaFreeAsync: %s", cudaGetErrorString(e2));
+    // buffer 0 now holds the post-collision state of step 1; the first step's
+    // "previous buffer" (its own input for readouts) is buffer 1, which gets the
+    // same role after the first rr_step.  Until then readouts are of the input.
+    s->cur = 0;
+    s->istep = 0;
+    s->ready = true;
+    s->stepped = false;
+    RR_CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+    if (where == RR_HOST) RR_CK(cudaStreamSynchronize(s->stream));
+    return RR_OK;
+}
+
+rr_status rr_step(rr_solver *s, int nsteps) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (!s->ready) return fail(RR_ERR_STATE, "rr_step before rr_init_state / rr_load");
+    if (nsteps < 0) return fail(RR_ERR_INVALID, "nsteps = %d", nsteps);
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    int left = nsteps;
+    if (left >= 2 * GRAPH_STEPS) {
+        if (s->cur != 0) {
+            rr_status st = launch_steps(s, 1);
+            if (st != RR_OK) return st;
+            left--;
+        }
+        rr_status st = build_graph(s);
+        if (st != RR_OK) return st;
+        while (left >= GRAPH_STEPS) {
+            RR_CK(cudaGraphLaunch(s->graph, s->stream));
+            left -= GRAPH_STEPS;
+        }
+    }
+    rr_status st = launch_steps(s, left);
+    if (st != RR_OK) return st;
+    s->istep += nsteps;
+    if (nsteps > 0) s->stepped = true;
+    return RR_OK;
+}
+
+rr_status rr_sync(rr_solver *s) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    int flag = 0;
+    RR_CK(cudaMemcpyAsync(&flag, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    RR_CK(cudaStreamSynchronize(s->stream));
+    if (flag) return fail(RR_ERR_WATCHDOG, "density left (0.1, 10) or became NaN by step %lld", s->istep);
+    return RR_OK;
+}
+
+long long rr_get_istep(const rr_solver *s) { return s ? s->istep : -1; }
+
+void *rr_get_stream(const rr_solver *s) { return s ? (void *)s->stream : nullptr; }
+
+size_t rr_device_bytes(const rr_solver *s) { return s ? s->bytes : 0; }
+
+rr_status rr_macro(rr_solver *s, double *rho, double *ux, double *uy, double *uz, double *taut,
+                   int where) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (!s->ready) return fail(RR_ERR_STATE, "no state");
+    if (!s->stepped) return fail(RR_ERR_STATE, "rr_macro needs a step after the state was set");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    rr_status st = readout_macros(s, taut != nullptr);
+    if (st != RR_OK) return st;
+    const size_t n = s->g.n;
+    double *dst[5] = {rho, ux, uy, uz, taut};
+    for (int k = 0; k < 5; k++)
+        if ((st = copy_out(s, dst[k], s->aux + k * n, n, where)) != RR_OK) return st;
+    return rr_sync(s);
+}
+
+rr_status rr_get_f(rr_solver *s, double *f, int where) {
+    if (!s || !f) return fail(RR_ERR_INVALID, "NULL argument");
+    if (!s->ready) return fail(RR_ERR_STATE, "no state");
+    if (!s->stepped) return fail(RR_ERR_STATE, "rr_get_f needs a step after the state was set");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    const size_t n = s->g.n, nf = (size_t)s->p.q * n;
+    double *dst = f;
+    double *tmp = nullptr;
+    if (where != RR_DEVICE) {
+        RR_CK(cudaMallocAsync(&tmp, nf * sizeof(double), s->stream));
+        dst = tmp;
+    }
+    cudaError_t e = s->ops->readout(s->p.q, has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, dst,
+                                    n, s->pos, nullptr, nullptr, nullptr, nullptr, s->stream);
+    if (e == cudaSuccess && tmp) e = cudaMemcpyAsync(f, tmp, nf * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+    if (tmp) cudaFreeAsync(tmp, s->stream);
+    if (e != cudaSuccess) return fail(RR_ERR_CUDA, "readout failed: %s", cudaGetErrorString(e));
+    return rr_sync(s);
+}
+
+rr_status rr_diag(rr_solver *s, double out[4]) {
+    if (!s || !out) return fail(RR_ERR_INVALID, "NULL argument");
+    if (!s->ready || !s->stepped) return fail(RR_ERR_STATE, "rr_diag needs a step after the state was set");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    rr_status st = readout_macros(s, false);
+    if (st != RR_OK) return st;
+    const size_t n = s->g.n;
+    double *partial = s->stat, *res = s->stat + 4 * rr::DIAG_MAX_BLOCKS;
+    RR_CK(rr::launch_diag(s->g.n, s->aux + n, s->aux + 2 * n, s->aux + 3 * n, s->aux, partial, res, s->stream));
+    RR_CK(cudaMemcpyAsync(out, res, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    return rr_sync(s);
+}
+
+static rr_status profile_device(rr_solver *s, double **prof) {
+    rr_status st = readout_macros(s, s->p.use_les != 0);
+    if (st != RR_OK) return st;
+    const size_t n = s->g.n;
+    *prof = s->stat + 4 * rr::DIAG_MAX_BLOCKS + 4;
+    RR_CK(rr::launch_profile(s->g, s->p.ystar, s->aux + n, s->aux + 2 * n, s->aux + 3 * n,
+                             s->p.use_les ? s->aux + 4 * n : nullptr, *prof, s->stream));
+    return RR_OK;
+}
+
+rr_status rr_profile(rr_solver *s, double *out) {
+    if (!s || !out) return fail(RR_ERR_INVALID, "NULL argument");
+    if (!s->ready || !s->stepped) return fail(RR_ERR_STATE, "rr_profile needs a step after the state was set");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    double *prof;
+    rr_status st = profile_device(s, &prof);
+    if (st != RR_OK) return st;
+    RR_CK(cudaMemcpyAsync(out, prof, 12 * (size_t)s->p.ly * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    return rr_sync(s);
+}
+
+rr_status rr_accumulate(rr_solver *s) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (!s->ready || !s->stepped) return fail(RR_ERR_STATE, "rr_accumulate needs a step after the state was set");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    double *prof;
+    rr_status st = profile_device(s, &prof);
+    if (st != RR_OK) return st;
+    const int m = 12 * s->p.ly;
+    RR_CK(rr::launch_accumulate(m, prof, prof + m, s->stream));
+    s->acc_samples++;
+    return RR_OK;
+}
+
+rr_status rr_get_accum(rr_solver *s, double *sums, long long *samples) {
+    if (!s || !sums) return fail(RR_ERR_INVALID, "NULL argument");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    const int m = 12 * s->p.ly;
+    double *acc = s->stat + 4 * rr::DIAG_MAX_BLOCKS + 4 + m;
+    RR_CK(cudaMemcpyAsync(sums, acc, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    if (samples) *samples = s->acc_samples;
+    return rr_sync(s);
+}
+
+rr_status rr_output(rr_solver *s, unsigned what, const char *dir) {
+    if (!s || !dir) return fail(RR_ERR_INVALID, "NULL argument");
+    rr_status st = ensure_dir(dir);
+    if (st != RR_OK) return st;
+    const size_t n = s->g.n;
+    const std::string d(dir);
+    char name[64];
+    if (what & RR_OUT_DIAG) {
+        // diag_flow, output.cu:37-56
+        double m[4];
+        if ((st = rr_diag(s, m)) != RR_OK) return st;
+        printf("Step %-7lld umean = %.17e, vmean = %.17e, wmean = %.17e, rhomean = %14.6e\n", s->istep,
+               m[0] / s->p.ustar, m[1], m[2], m[3]);
+        fflush(stdout);
+        char line[256];
+        int len = snprintf(line, sizeof line, "%-7lld %14.6e %14.6e %14.6e %14.6e\n", s->istep, m[0], m[1], m[2], m[3]);
+        if ((st = write_file(d + "/statistics.dat", line, (size_t)len, "a")) != RR_OK) return st;
+    }
+    if (what & (RR_OUT_FLOW)) {
+        // output_flow, output.cu:89-131: rho, ux, uy, uz FP64 back to back
+        std::vector<double> h(4 * n);
+        if ((st = rr_macro(s, h.data(), h.data() + n, h.data() + 2 * n, h.data() + 3 * n, nullptr, RR_HOST)) != RR_OK)
+            return st;
+        snprintf(name, sizeof name, "/%09lld.dat", s->istep);
+        if ((st = write_file(d + name, h.data(), 4 * n * sizeof(double), "wb")) != RR_OK) return st;
+    }
+    if (what & RR_OUT_PROFILE) {
+        // output_profile, output.cu:158-214.  The reference passes iy + 0.5 to
+        // a "%d" conversion (output.cu:213-214): on x86-64 and aarch64 the %d
+        // then reads an unrelated integer register and the eleven %e
+        // conversions print the first eleven doubles (iy + 0.5 ... <v'w'>),
+        // leaving <tau_t> unprinted.  Those are the columns written here, with
+        // iy in place of the unspecified integer; rr_profile() returns <tau_t>.
+        std::vector<double> pr(12 * (size_t)s->p.ly);
+        if ((st = rr_profile(s, pr.data())) != RR_OK) return st;
+        std::string txt = std::to_string(s->istep) + "\n";
+        char line[512];
+        for (int iy = 0; iy < s->p.ly; iy++) {
+            const double *o = pr.data() + 11 * (size_t)iy;
+            snprintf(line, sizeof line,
+                     "%d, %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e\n", iy,
+                     o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7], o[8], o[9], o[10]);
+            txt += line;
+        }
+        if ((st = write_file(d + "/Profiles.txt", txt.data(), txt.size(), "a")) != RR_OK) return st;
+    }
+    if (what & RR_OUT_F) {
+        // output_f, output.cu:227-258
+        std::vector<double> h((size_t)s->p.q * n);
+        if ((st = rr_get_f(s, h.data(), RR_HOST)) != RR_OK) return st;
+        snprintf(name, sizeof name, "/f%09lld.dat", s->istep);
+        if ((st = write_file(d + name, h.data(), h.size() * sizeof(double), "wb")) != RR_OK) return st;
+    }
+    return RR_OK;
+}
+
+rr_status rr_save(rr_solver *s, const char *dir) { return rr_output(s, RR_OUT_FLOW | RR_OUT_F, dir); }
+
+rr_status rr_load(rr_solver *s, const char *dir, long long istep) {
+    // initialize() with CONTINUE_STEP > 0, initial.cu:189-265
+    if (!s || !dir) return fail(RR_ERR_INVALID, "NULL argument");
+    const size_t n = s->g.n, nf = (size_t)s->p.q * n;
+    std::vector<double> m(4 * n), f(nf);
+    char name[64];
+    auto rd = [&](const std::string &path, double *dst, size_t count) -> rr_status {
+        FILE *fp = fopen(path.c_str(), "rb");
+        if (!fp) return fail(RR_ERR_IO, "cannot open file: %s", path.c_str());
+        size_t r = fread(dst, sizeof(double), count, fp);
+        fclose(fp);
+        if (r != count) return fail(RR_ERR_IO, "%s: read %zu of %zu elements", path.c_str(), r, count);
+        return RR_OK;
+    };
+    snprintf(name, sizeof name, "/%09lld.dat", istep);
+    rr_status st = rd(std::string(dir) + name, m.data(), 4 * n);
+    if (st != RR_OK) return st;
+    snprintf(name, sizeof name, "/f%09lld.dat", istep);
+    if ((st = rd(std::string(dir) + name, f.data(), nf)) != RR_OK) return st;
+    if ((st = rr_init_state(s, f.data(), m.data(), m.data() + n, m.data() + 2 * n, m.data() + 3 * n, RR_HOST)) != RR_OK)
+        return st;
+    s->istep = istep;
+    return RR_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,48 @@
+// rr_dispatch.h -- host-side launch table, one per population storage type.
+// Each rr_inst_<type>.cu instantiates the kernels of rr_kernels.cuh for its
+// storage type and fills one Ops table; rr_api.cu picks the table at
+// rr_create time.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace rr {
+
+struct Geom;
+
+struct LesTile {
+    int tx, ty, zchunk; // tile of the WALE step kernel (autotuned per size class)
+};
+
+struct Ops {
+    size_t elem_bytes;
+    // one fused time step: fin -> fout
+    cudaError_t (*step)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
+                        const double F[3], int *status, cudaStream_t st);
+    // fused time step with the WALE eddy viscosity
+    cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
+                            double tau, double cw, const double F[3], int *status,
+                            const LesTile &tile, cudaStream_t st);
+    // post-stream populations / macroscopic fields from the post-collision buffer
+    cudaError_t (*readout)(int q, bool force, const void *fin, const Geom &g, const double F[3],
+                           double *fo, unsigned long long fo_stride, const int *pos, double *rho,
+                           double *ux, double *uy, double *uz, cudaStream_t st);
+    // state upload + first collision with given macros
+    cudaError_t (*upload)(int q, bool force, void *fout, const Geom &g, double tau,
+                          const double F[3], const double *fi, unsigned long long fi_stride,
+                          const int *pos, const double *rho, const double *ux, const double *uy,
+                          const double *uz, const double *taut, cudaStream_t st);
+};
+
+const Ops &ops_f64();
+const Ops &ops_f32();
+const Ops &ops_f16();
+const Ops &ops_bf16();
+
+// FP64 helpers shared by all storage types (rr_aux.cu)
+cudaError_t launch_wale(const Geom &g, double cw, const double *ux, const double *uy,
+                        const double *uz, double *taut, cudaStream_t st);
+
+} // namespace rr

@@ -1,0 +1,6 @@
+// kernels for __nv_bfloat16 population storage (see rr_inst.inc)
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#define RR_STORE __nv_bfloat16
+#define RR_OPS_NAME ops_bf16
+#include "rr_inst.inc"

@@ -1,0 +1,252 @@
+// rr_kernels.cuh -- the fused RR-LBM time step and its companions.
+//
+// State in HBM: one array per population ("SoA"), f_i of node
+// (x, y, z) at fin[i * stride + (z * ny + y) * nx + x], stored as the
+// deviation d_i = f_i / w_i - 1 in FP64, FP32, FP16 or BF16.  Two such arrays
+// ping-pong: a step reads the post-collision state of the previous step and
+// writes its own.
+//
+// One step (one launch) per node, in the reference's order (main.cu:360-409):
+//   pull-stream from the neighbours with periodic wrap  (streaming.cu:3-24)
+//   wall faces x-lo, x-hi, y-lo, y-hi, z-lo, z-hi in that order:
+//     half-way bounce-back with moving-wall term         (BB, streaming.cu:26-56;
+//                                                         Cavity/streaming.f90:91-152)
+//     regularized closure of the entering populations    (RRBC, BC.cu:4-126)
+//   moments rho, u = (sum c f + F/2) / rho               (macrovar.cu:4-31)
+//   [WALE eddy viscosity from the neighbours' velocities] (LES.cu:4-98)
+//   RR collision                                         (collision.cu:4-120)
+// The reference runs the collision first and the streaming last; the fused
+// kernel runs the same sequence shifted by half a step, so its state is the
+// post-collision one.  The macroscopic fields the reference holds after step
+// n are produced on demand by readout_kernel (pull + walls + moments from the
+// previous buffer).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "rr_node.cuh"
+
+namespace rr {
+
+enum FaceKind : int { FACE_PERIODIC = 0, FACE_WALL = 1, FACE_WALL_BB = 2 };
+
+struct Geom {
+    int nx, ny, nz;
+    uint32_t n;          // nodes
+    unsigned long long stride; // elements between population arrays (>= n)
+    int face[6];         // FaceKind of x-lo, x-hi, y-lo, y-hi, z-lo, z-hi
+    double uw[6][3];     // wall velocity of each face
+    uint32_t wallmask;   // bit f: face f is a wall
+};
+
+template <typename S> struct CType { using T = float; };
+template <> struct CType<double> { using T = double; };
+
+template <typename T> __device__ __forceinline__ T ld_dev(const double *p) { return T(*p); }
+template <typename T> __device__ __forceinline__ T ld_dev(const float *p) { return T(*p); }
+template <typename T> __device__ __forceinline__ T ld_dev(const __half *p) { return T(__half2float(*p)); }
+template <typename T> __device__ __forceinline__ T ld_dev(const __nv_bfloat16 *p) {
+    return T(__bfloat162float(*p));
+}
+template <typename T> __device__ __forceinline__ void st_dev(double *p, T v) { *p = double(v); }
+template <typename T> __device__ __forceinline__ void st_dev(float *p, T v) { *p = float(v); }
+template <typename T> __device__ __forceinline__ void st_dev(__half *p, T v) { *p = __float2half_rn(float(v)); }
+template <typename T> __device__ __forceinline__ void st_dev(__nv_bfloat16 *p, T v) {
+    *p = __float2bfloat16_rn(float(v));
+}
+
+__device__ __forceinline__ void node_xyz(uint32_t idx, int nx, int ny, int &x, int &y, int &z) {
+    uint32_t t = idx / (uint32_t)nx;
+    x = (int)(idx - t * (uint32_t)nx);
+    z = (int)(t / (uint32_t)ny);
+    y = (int)(t - (uint32_t)z * (uint32_t)ny);
+}
+
+// pull every population from its upstream neighbour, periodic wrap on all axes
+// (walls overwrite the wrapped values afterwards, as in the reference)
+template <class LT, typename S, typename T>
+__device__ __forceinline__ void pull(const S *__restrict__ fin, unsigned long long stride, int nx,
+                                     int ny, int nz, int x, int y, int z, T (&d)[LT::Q]) {
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const int zm = z == 0 ? nz - 1 : z - 1, zp = z == nz - 1 ? 0 : z + 1;
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        constexpr int cx = LT::cx(i), cy = LT::cy(i), cz = LT::cz(i);
+        const int xs = cx > 0 ? xm : (cx < 0 ? xp : x);
+        const int ys = cy > 0 ? ym : (cy < 0 ? yp : y);
+        const int zs = cz > 0 ? zm : (cz < 0 ? zp : z);
+        const uint32_t src = ((uint32_t)zs * (uint32_t)ny + (uint32_t)ys) * (uint32_t)nx + (uint32_t)xs;
+        d[i] = ld_dev<T>(fin + (unsigned long long)i * stride + src);
+    });
+}
+
+__device__ __forceinline__ bool on_face(int f, int x, int y, int z, const Geom &g) {
+    switch (f) {
+    case 0: return x == 0;
+    case 1: return x == g.nx - 1;
+    case 2: return y == 0;
+    case 3: return y == g.ny - 1;
+    case 4: return z == 0;
+    default: return z == g.nz - 1;
+    }
+}
+
+__device__ __forceinline__ bool any_wall(int x, int y, int z, const Geom &g) {
+    const uint32_t m = g.wallmask;
+    return ((m & 1u) && x == 0) || ((m & 2u) && x == g.nx - 1) || ((m & 4u) && y == 0) ||
+           ((m & 8u) && y == g.ny - 1) || ((m & 16u) && z == 0) || ((m & 32u) && z == g.nz - 1);
+}
+
+// wall faces in the reference order: bounce-back from the post-collision
+// opposite population of this node plus 6 c_i.U_wall (in deviation form
+// d_i = d*_ibar + 6 c_i.U), then the regularized closure of the same
+// populations when the face is FACE_WALL
+template <class LT, typename S, typename T, bool FORCE>
+__device__ __forceinline__ void wall_pass(const S *__restrict__ fin, const Geom &g, uint32_t idx, int x,
+                                       int y, int z, T (&d)[LT::Q], T Fx, T Fy, T Fz) {
+#pragma unroll 1
+    for (int f = 0; f < 6; f++) {
+        if (!((g.wallmask >> f) & 1u) || !on_face(f, x, y, z, g)) continue;
+        const int axis = f >> 1;
+        const bool hi = f & 1;
+        const T ux = T(g.uw[f][0]), uy = T(g.uw[f][1]), uz = T(g.uw[f][2]);
+        uint32_t mask = 0;
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int o = LT::opp(i);
+            const int c = axis == 0 ? LT::cx(i) : (axis == 1 ? LT::cy(i) : LT::cz(i));
+            const bool ent = hi ? (c < 0) : (c > 0);
+            if (ent) {
+                mask |= 1u << i;
+                T v = ld_dev<T>(fin + (unsigned long long)o * g.stride + idx);
+                d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+            }
+        });
+        if (g.face[f] == FACE_WALL) regularize<LT, T, FORCE>(d, mask, Fx, Fy, Fz);
+    }
+}
+
+template <typename S>
+struct StepArgs {
+    const S *__restrict__ fin;
+    S *__restrict__ fout;
+    Geom g;
+    double om1;       // 1 - 1/tau
+    double F[3];      // uniform body force
+    int *status;      // watchdog flag (bit 0: density out of range / NaN)
+};
+
+// DNS step: one thread per node
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
+    using T = typename CType<S>::T;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.g.n) return;
+    int x, y, z;
+    node_xyz(idx, a.g.nx, a.g.ny, x, y, z);
+    T d[LT::Q];
+    pull<LT>(a.fin, a.g.stride, a.g.nx, a.g.ny, a.g.nz, x, y, z, d);
+    const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    if (a.g.wallmask && any_wall(x, y, z, a.g)) wall_pass<LT, S, T, FORCE>(a.fin, a.g, idx, x, y, z, d, Fx, Fy, Fz);
+    Mom<T> m = moments<LT>(d);
+    T ux, uy, uz;
+    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        st_dev<T>(a.fout + (unsigned long long)i * a.g.stride + idx, d[i]);
+    });
+}
+
+// Readout: the reference's post-stream state after the last step, from the
+// previous post-collision buffer.  Writes FP64 f (reference layout, ordering
+// given by pos: internal population i goes to output population pos[i]) and/or the
+// macroscopic fields.
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256)
+readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double Fz_,
+               double *__restrict__ fo, unsigned long long fo_stride, const int *__restrict__ pos,
+               double *__restrict__ rho, double *__restrict__ ux_o, double *__restrict__ uy_o,
+               double *__restrict__ uz_o) {
+    using T = typename CType<S>::T;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.n) return;
+    int x, y, z;
+    node_xyz(idx, g.nx, g.ny, x, y, z);
+    T d[LT::Q];
+    pull<LT>(fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+    const T Fx = T(Fx_), Fy = T(Fy_), Fz = T(Fz_);
+    if (g.wallmask && any_wall(x, y, z, g)) wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
+    if (fo) {
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            fo[(unsigned long long)pos[i] * fo_stride + idx] = LT::w(i) * (1.0 + double(d[i]));
+        });
+    }
+    if (rho) {
+        // moments in FP64 from the stored state (macrovar.cu:18-28)
+        double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const double fv = LT::w(i) * (1.0 + double(d[i]));
+            r += fv;
+            if constexpr (LT::cx(i) > 0) jx += fv;
+            if constexpr (LT::cx(i) < 0) jx -= fv;
+            if constexpr (LT::cy(i) > 0) jy += fv;
+            if constexpr (LT::cy(i) < 0) jy -= fv;
+            if constexpr (LT::cz(i) > 0) jz += fv;
+            if constexpr (LT::cz(i) < 0) jz -= fv;
+        });
+        rho[idx] = r;
+        ux_o[idx] = (jx + 0.5 * Fx_) / r;
+        uy_o[idx] = (jy + 0.5 * Fy_) / r;
+        uz_o[idx] = (jz + 0.5 * Fz_) / r;
+    }
+}
+
+// State upload: populations in the reference's post-stream form (FP64,
+// reference layout; internal population i is input population pos[i]) plus the macroscopic fields the first
+// collision is to use (init_arrays, initial.cu:268-326, stores macros that
+// are not the moments of f).  Collides and writes the post-collision state.
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256)
+upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, double Fz_,
+              const double *__restrict__ fi, unsigned long long fi_stride, const int *__restrict__ pos,
+              const double *__restrict__ rho, const double *__restrict__ ux,
+              const double *__restrict__ uy, const double *__restrict__ uz,
+              const double *__restrict__ taut) {
+    using T = typename CType<S>::T;
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.n) return;
+    T d[LT::Q];
+    if (fi) {
+        // internal population i is input population pos[i]
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            d[i] = T(fi[(unsigned long long)pos[i] * fi_stride + idx] / LT::w(i) - 1.0);
+        });
+    } else {
+        // second-order equilibrium of (rho, u), Cavity/collision.f90:103-114:
+        // feq = w rho (1 + eu + (eu^2 - uv)/2), eu = c.u / cs^2, uv = u.u / cs^2
+        const double r = rho[idx], u0 = ux[idx], u1 = uy[idx], u2 = uz[idx];
+        const double uv = 3.0 * (u0 * u0 + u1 * u1 + u2 * u2);
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const double eu = 3.0 * (LT::cx(i) * u0 + LT::cy(i) * u1 + LT::cz(i) * u2);
+            d[i] = T((r - 1.0) + r * (eu + 0.5 * (eu * eu - uv)));
+        });
+    }
+    Mom<T> m = moments<LT>(d);
+    const double tau_eff = taut ? tau + taut[idx] : tau;
+    collide<LT, T, FORCE>(d, m, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]),
+                          T(1.0 - 1.0 / tau_eff), T(Fx_), T(Fy_), T(Fz_));
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        st_dev<T>(fout + (unsigned long long)i * g.stride + idx, d[i]);
+    });
+}
+
+} // namespace rr

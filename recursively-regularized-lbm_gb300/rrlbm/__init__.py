@@ -1,0 +1,234 @@
+"""rrlbm -- Python front end of librrlbm.so (include/rr_api.h).
+
+Mirrors the reference's host interface: the knobs of
+RR27V33_code_DNS_LES/parameters.h and globals.cu live in :class:`Params`; a
+:class:`Solver` is the state of ``initialize()`` (initial.cu:4-266); ``step``
+is one pass of the time loop body (main.cu:360-409); ``output`` writes the
+reference's files (output.cu).  Every call goes through the C ABI; there is no
+CPU fallback: without the built library or a CUDA device the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "librrlbm.so")
+
+STORE_F64, STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2, 3
+STORAGE = {"f64": STORE_F64, "f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
+FACE_PERIODIC, FACE_WALL, FACE_WALL_BB = 0, 1, 2
+ORDER_CUDA, ORDER_FORTRAN = 0, 1
+HOST, DEVICE = 0, 1
+OUT_DIAG, OUT_FLOW, OUT_PROFILE, OUT_F = 1, 2, 4, 8
+
+STATUS = {0: "RR_OK", 1: "RR_ERR_INVALID", 2: "RR_ERR_CUDA", 3: "RR_ERR_NOMEM",
+          4: "RR_ERR_UNSUPPORTED", 5: "RR_ERR_WATCHDOG", 6: "RR_ERR_IO", 7: "RR_ERR_STATE"}
+
+
+class RRError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """rr_params: run-time counterpart of parameters.h:1-25 / globals.cu:18-40."""
+    _fields_ = [("lx", ctypes.c_int), ("ly", ctypes.c_int), ("lz", ctypes.c_int),
+                ("q", ctypes.c_int), ("use_les", ctypes.c_int), ("tau", ctypes.c_double),
+                ("cw", ctypes.c_double), ("force", ctypes.c_double * 3),
+                ("face", ctypes.c_int * 6), ("uwall", (ctypes.c_double * 3) * 6),
+                ("storage", ctypes.c_int), ("order", ctypes.c_int), ("device", ctypes.c_int),
+                ("ustar", ctypes.c_double), ("ystar", ctypes.c_double)]
+
+    @property
+    def n(self):
+        return self.lx * self.ly * self.lz
+
+    @property
+    def shape(self):
+        return (self.lz, self.ly, self.lx)
+
+
+_LIB = None
+
+
+def lib():
+    """The loaded C library (raises if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError(f"{LIBPATH} missing: build it with rrlbm/build.py (nvcc, sm_103a)")
+        L = ctypes.CDLL(LIBPATH)
+        vp, dp, P = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(Params)
+        sig = {
+            "rr_params_default": ([P], ctypes.c_int),
+            "rr_create": ([P, ctypes.POINTER(vp)], ctypes.c_int),
+            "rr_destroy": ([vp], ctypes.c_int),
+            "rr_init_state": ([vp, vp, vp, vp, vp, vp, ctypes.c_int], ctypes.c_int),
+            "rr_step": ([vp, ctypes.c_int], ctypes.c_int),
+            "rr_sync": ([vp], ctypes.c_int),
+            "rr_get_istep": ([vp], ctypes.c_longlong),
+            "rr_get_stream": ([vp], ctypes.c_void_p),
+            "rr_macro": ([vp, vp, vp, vp, vp, vp, ctypes.c_int], ctypes.c_int),
+            "rr_get_f": ([vp, vp, ctypes.c_int], ctypes.c_int),
+            "rr_diag": ([vp, dp], ctypes.c_int),
+            "rr_profile": ([vp, dp], ctypes.c_int),
+            "rr_accumulate": ([vp], ctypes.c_int),
+            "rr_get_accum": ([vp, dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+            "rr_output": ([vp, ctypes.c_uint, ctypes.c_char_p], ctypes.c_int),
+            "rr_save": ([vp, ctypes.c_char_p], ctypes.c_int),
+            "rr_load": ([vp, ctypes.c_char_p, ctypes.c_longlong], ctypes.c_int),
+            "rr_device_bytes": ([vp], ctypes.c_size_t),
+            "rr_bytes_for": ([P], ctypes.c_size_t),
+            "rr_last_error": ([], ctypes.c_char_p),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def _check(code):
+    if code != 0:
+        raise RRError(code, lib().rr_last_error().decode())
+
+
+def params_default():
+    """parameters.h + globals.cu defaults (64^3 Re_tau=180 channel, DNS, FP64)."""
+    p = Params()
+    _check(lib().rr_params_default(ctypes.byref(p)))
+    return p
+
+
+def bytes_for(p):
+    return lib().rr_bytes_for(ctypes.byref(p))
+
+
+def _ptr(a):
+    """(pointer, where) of a numpy array or a CUDA tensor (torch / __cuda_array_interface__)."""
+    if a is None:
+        return None, HOST
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("arrays crossing the API are C-contiguous float64")
+        return a.ctypes.data, HOST
+    cai = getattr(a, "__cuda_array_interface__", None)
+    if cai is not None:
+        if cai["typestr"] != "<f8":
+            raise ValueError("device arrays crossing the API are float64")
+        return cai["data"][0], DEVICE
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+class Solver:
+    """One domain resident in HBM (rr_solver)."""
+
+    def __init__(self, params):
+        self.p = params
+        h = ctypes.c_void_p()
+        _check(lib().rr_create(ctypes.byref(params), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state ---------------------------------------------------------------
+    def init_state(self, rho, ux, uy, uz, f=None):
+        """initialize(): post-stream populations f (q x N, or None for the
+        second-order equilibrium) and the macros the first collision uses."""
+        ptrs = [_ptr(a) for a in (f, rho, ux, uy, uz)]
+        where = ptrs[1][1]
+        if any(w != where for p_, w in ptrs if p_ is not None):
+            raise ValueError("all arrays on the host or all on the device")
+        _check(lib().rr_init_state(self._h, *[p_ for p_, _ in ptrs], where))
+
+    def step(self, n=1):
+        _check(lib().rr_step(self._h, int(n)))
+
+    def sync(self):
+        _check(lib().rr_sync(self._h))
+
+    @property
+    def istep(self):
+        return lib().rr_get_istep(self._h)
+
+    @property
+    def stream(self):
+        """the solver's cudaStream_t as an integer handle"""
+        return lib().rr_get_stream(self._h) or 0
+
+    @property
+    def device_bytes(self):
+        return lib().rr_device_bytes(self._h)
+
+    # -- readouts --------------------------------------------------------------
+    def macro(self, taut=False):
+        shp = self.p.shape
+        out = {k: np.empty(shp) for k in ("rho", "ux", "uy", "uz")}
+        if taut:
+            out["taut"] = np.empty(shp)
+        args = [out[k].ctypes.data if k in out else None for k in ("rho", "ux", "uy", "uz", "taut")]
+        _check(lib().rr_macro(self._h, *args, HOST))
+        return out
+
+    def macro_into(self, rho, ux, uy, uz, taut=None):
+        ptrs = [_ptr(a) for a in (rho, ux, uy, uz, taut)]
+        where = ptrs[0][1]
+        _check(lib().rr_macro(self._h, *[p_ for p_, _ in ptrs], where))
+
+    def get_f(self):
+        f = np.empty((self.p.q,) + self.p.shape)
+        _check(lib().rr_get_f(self._h, f.ctypes.data, HOST))
+        return f
+
+    def diag(self):
+        out = (ctypes.c_double * 4)()
+        _check(lib().rr_diag(self._h, out))
+        return np.array(out[:])
+
+    def profile(self):
+        ly = self.p.ly
+        out = np.empty(12 * ly)
+        _check(lib().rr_profile(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out[: 11 * ly].reshape(ly, 11), out[11 * ly:]
+
+    def accumulate(self):
+        _check(lib().rr_accumulate(self._h))
+
+    def get_accum(self):
+        ly = self.p.ly
+        out = np.empty(12 * ly)
+        n = ctypes.c_longlong()
+        _check(lib().rr_get_accum(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  ctypes.byref(n)))
+        return out[: 11 * ly].reshape(ly, 11), out[11 * ly:], n.value
+
+    # -- files -------------------------------------------------------------------
+    def output(self, what, directory="data"):
+        _check(lib().rr_output(self._h, int(what), directory.encode()))
+
+    def save(self, directory):
+        _check(lib().rr_save(self._h, directory.encode()))
+
+    def load(self, directory, istep):
+        _check(lib().rr_load(self._h, directory.encode(), int(istep)))
+
+
+from . import presets  # noqa: E402,F401
