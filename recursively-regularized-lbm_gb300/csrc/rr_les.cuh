@@ -44,7 +44,7 @@ __device__ __forceinline__ T wale_tau_t(const T (&gr)[3][3], T cw) {
     T s33d = (T(2) * dwdz * dwdz - dudx * dudx - dvdy * dvdy + dudz * dwdx + dvdz * dwdy - T(2) * dudy * dvdx) * third;
     T sd = s11d * s11d + s22d * s22d + s33d * s33d + T(2) * (s12d * s12d + s13d * s13d + s23d * s23d);
     const T rs = rr_sqrt(sijsq), rd = rr_sqrt(sd);
-    const T den = sijsq * sijsq * rs + rd * rr_sqrt(rd);
+    const T den = sijsq * sijsq * rs + sd * rr_sqrt(rd); // S:S^2.5 + Sd:Sd^1.25
     return den > T(0) ? T(3) * cw * cw * (sd * rd) / den : T(0);
 }
 
