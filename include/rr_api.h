@@ -60,6 +60,11 @@ typedef enum {
  * (the only ordering defined for D3Q19, Taylor_Green/D3Q19RR.f90:75-77) */
 typedef enum { RR_ORDER_CUDA = 0, RR_ORDER_FORTRAN = 1 } rr_order;
 
+/* rounding of FP16/BF16 population stores (no effect on FP32/FP64 storage):
+ * stochastic rounding is unbiased, so population changes smaller than half a
+ * unit in the last place accumulate instead of stalling */
+typedef enum { RR_ROUND_NEAREST = 0, RR_ROUND_STOCHASTIC = 1 } rr_rounding;
+
 /* where a caller buffer lives */
 typedef enum { RR_HOST = 0, RR_DEVICE = 1 } rr_where;
 
@@ -83,6 +88,7 @@ typedef struct rr_params {
     int order;           /* rr_order of populations crossing the API */
     int device;          /* CUDA device ordinal */
     double ustar, ystar; /* friction velocity and viscous length, for output_profile's y+ */
+    int rounding;        /* rr_rounding of FP16/BF16 stores (default stochastic) */
 } rr_params;
 
 typedef struct rr_solver rr_solver;

@@ -86,6 +86,8 @@ rr_status validate(const rr_params *p) {
         (p->face[4] == RR_FACE_PERIODIC) != (p->face[5] == RR_FACE_PERIODIC))
         return fail(RR_ERR_INVALID, "an axis must be periodic on both faces or on neither");
     if (p->use_les && !(p->cw >= 0.0)) return fail(RR_ERR_INVALID, "cw = %g", p->cw);
+    if (p->rounding != RR_ROUND_NEAREST && p->rounding != RR_ROUND_STOCHASTIC)
+        return fail(RR_ERR_INVALID, "rounding = %d unknown", p->rounding);
     return RR_OK;
 }
 
@@ -108,6 +110,10 @@ struct rr_solver {
     long long acc_samples = 0;
     size_t bytes = 0;
     rr::LesTile tile{32, 8, 16};
+    rr::StepRange box{};     // nodes off every wall face: launch without wall code
+    rr::StepRange shell{};   // wall-face nodes, by index list
+    uint32_t *shell_list = nullptr;
+    int block = 256;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -171,11 +177,15 @@ rr_status launch_steps(rr_solver *s, int n) {
     for (int k = 0; k < n; k++) {
         const void *fin = s->buf[s->cur];
         void *fout = s->buf[1 - s->cur];
-        if (s->p.use_les)
+        if (s->p.use_les) {
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
                                    s->status, s->tile, s->stream));
-        else
-            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->stream));
+        } else {
+            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->box,
+                               s->block, s->stream));
+            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->shell,
+                               s->block, s->stream));
+        }
         s->cur = 1 - s->cur;
     }
     return RR_OK;
@@ -243,6 +253,7 @@ rr_status rr_params_default(rr_params *p) {
     p->device = 0;
     p->ustar = u0;
     p->ystar = visc / u0;
+    p->rounding = RR_ROUND_STOCHASTIC;
     return RR_OK;
 }
 
@@ -310,6 +321,48 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
     }
     s->bytes += 256 + sd;
+    // interior box (nodes on no wall face) and the shell list of wall-face nodes
+    {
+        const int n3[3] = {p->lx, p->ly, p->lz};
+        int lo[3], ext[3];
+        for (int a = 0; a < 3; a++) {
+            const bool wall = p->face[2 * a] != RR_FACE_PERIODIC;
+            lo[a] = wall ? 1 : 0;
+            ext[a] = wall ? n3[a] - 2 : n3[a];
+            if (ext[a] < 0) ext[a] = 0;
+        }
+        s->box.mode = rr::MODE_BOX;
+        s->box.count = (uint32_t)ext[0] * (uint32_t)ext[1] * (uint32_t)ext[2];
+        for (int a = 0; a < 3; a++) s->box.lo[a] = lo[a];
+        s->box.ex = (uint32_t)ext[0];
+        s->box.exy = (uint32_t)ext[0] * (uint32_t)ext[1];
+        s->box.list = nullptr;
+        std::vector<uint32_t> shell;
+        shell.reserve(g.n - s->box.count);
+        for (int z = 0; z < p->lz; z++)
+            for (int y = 0; y < p->ly; y++)
+                for (int x = 0; x < p->lx; x++) {
+                    const bool in = x >= lo[0] && x < lo[0] + ext[0] && y >= lo[1] && y < lo[1] + ext[1] &&
+                                    z >= lo[2] && z < lo[2] + ext[2];
+                    if (!in) shell.push_back(((uint32_t)z * p->ly + y) * p->lx + x);
+                }
+        s->shell.mode = rr::MODE_LIST;
+        s->shell.count = (uint32_t)shell.size();
+        s->shell.list = nullptr;
+        if (!shell.empty()) {
+            const size_t lb = shell.size() * sizeof(uint32_t);
+            if (cudaMalloc(&s->shell_list, lb) != cudaSuccess) {
+                cudaGetLastError();
+                s->shell_list = nullptr;
+                return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the wall-node list"));
+            }
+            if (cudaMemcpy(s->shell_list, shell.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+                return cleanup(fail(RR_ERR_CUDA, "cannot upload the wall-node list"));
+            s->shell.list = s->shell_list;
+            s->bytes += lb;
+        }
+    }
+    g.sround = (p->rounding == RR_ROUND_STOCHASTIC) ? 1 : 0;
     // LES tile by size class: full 32-wide rows when x allows, else 16
     s->tile.tx = p->lx >= 32 ? 32 : 16;
     s->tile.ty = 256 / s->tile.tx;
@@ -328,6 +381,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->status);
     cudaFree(s->aux);
     cudaFree(s->stat);
+    cudaFree(s->shell_list);
     if (s->stream) cudaStreamDestroy(s->stream);
     cudaGetLastError();
     delete s;

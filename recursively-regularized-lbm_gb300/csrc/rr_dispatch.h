@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 
 namespace rr {
 
@@ -16,11 +17,22 @@ struct LesTile {
     int tx, ty, zchunk; // tile of the WALE step kernel (autotuned per size class)
 };
 
+// nodes covered by one step launch: the box of nodes off every wall face
+// (mode 0) or the list of wall-face nodes (mode 1)
+struct StepRange {
+    int mode;
+    uint32_t count;
+    int lo[3];
+    uint32_t ex, exy;
+    const uint32_t *list;
+};
+
 struct Ops {
     size_t elem_bytes;
-    // one fused time step: fin -> fout
+    // one fused time step over the nodes of `r`: fin -> fout
     cudaError_t (*step)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
-                        const double F[3], int *status, cudaStream_t st);
+                        const double F[3], int *status, const StepRange &r, int block,
+                        cudaStream_t st);
     // fused time step with the WALE eddy viscosity
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,

@@ -38,6 +38,7 @@ struct Geom {
     int face[6];         // FaceKind of x-lo, x-hi, y-lo, y-hi, z-lo, z-hi
     double uw[6][3];     // wall velocity of each face
     uint32_t wallmask;   // bit f: face f is a wall
+    int sround;          // FP16/BF16 storage: stochastic (1) or nearest (0) rounding
 };
 
 template <typename S> struct CType { using T = float; };
@@ -54,6 +55,52 @@ template <typename T> __device__ __forceinline__ void st_dev(float *p, T v) { *p
 template <typename T> __device__ __forceinline__ void st_dev(__half *p, T v) { *p = __float2half_rn(float(v)); }
 template <typename T> __device__ __forceinline__ void st_dev(__nv_bfloat16 *p, T v) {
     *p = __float2bfloat16_rn(float(v));
+}
+
+// 32-bit integer finaliser (xor-shift / multiply), used as a counter-free
+// source of rounding noise
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// Stochastic rounding to 16 bits: r is added to the float bits that the
+// conversion drops (13 for FP16, 16 for BF16) before truncating, so the
+// magnitude is rounded up with probability (dropped fraction) / 2^bits and the
+// stored value is unbiased.  Round-to-nearest stalls a slowly varying field
+// whose per-step change is below half a unit in the last place (e.g. the
+// Ma = 0.01 Taylor-Green decay); unbiased rounding keeps that change in
+// expectation.  For FP16 subnormals the rounding is biased toward zero by less
+// than one subnormal step (6e-8).
+__device__ __forceinline__ __half f2h_sr(float v, uint32_t r) {
+    return __float2half_rz(__uint_as_float(__float_as_uint(v) + (r & 0x1FFFu)));
+}
+__device__ __forceinline__ __nv_bfloat16 f2bf_sr(float v, uint32_t r) {
+    return __float2bfloat16_rz(__uint_as_float(__float_as_uint(v) + (r & 0xFFFFu)));
+}
+
+// store a node's post-collision populations, coalesced across the warp
+template <class LT, typename S, typename T>
+__device__ __forceinline__ void store_node(S *__restrict__ fout, unsigned long long stride, uint32_t idx,
+                                           const T (&d)[LT::Q], bool sround) {
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        S *p = fout + (unsigned long long)i * stride + idx;
+        if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+            if (sround) {
+                // noise keyed by the value and the (node, population) slot
+                const uint32_t r = mix32(__float_as_uint(float(d[i])) ^ (idx * 0x9E3779B9u + (uint32_t)i * 0x85EBCA6Bu));
+                if constexpr (std::is_same<S, __half>::value) *p = f2h_sr(float(d[i]), r);
+                else *p = f2bf_sr(float(d[i]), r);
+                return;
+            }
+        }
+        st_dev<T>(p, d[i]);
+    });
 }
 
 __device__ __forceinline__ void node_xyz(uint32_t idx, int nx, int ny, int &x, int &y, int &z) {
@@ -128,6 +175,12 @@ __device__ __forceinline__ void wall_pass(const S *__restrict__ fin, const Geom 
     }
 }
 
+// Which nodes a step launch covers.  The nodes off every wall face form a box
+// (the whole grid for a periodic domain); a launch over that box carries no
+// wall code at all, so no warp diverges into the wall closure.  The remaining
+// wall-face nodes (the shell) go through a second launch over an index list.
+enum StepMode : int { MODE_BOX = 0, MODE_LIST = 1 };
+
 template <typename S>
 struct StepArgs {
     const S *__restrict__ fin;
@@ -136,29 +189,41 @@ struct StepArgs {
     double om1;       // 1 - 1/tau
     double F[3];      // uniform body force
     int *status;      // watchdog flag (bit 0: density out of range / NaN)
+    uint32_t count;   // nodes of this launch
+    int lo[3];        // MODE_BOX: first node of the box
+    uint32_t ex, exy; // MODE_BOX: box extent in x, and in x*y
+    const uint32_t *__restrict__ list; // MODE_LIST: node indices
 };
 
 // DNS step: one thread per node
-template <class LT, typename S, bool FORCE>
+template <class LT, typename S, bool FORCE, int MODE>
 __global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
     using T = typename CType<S>::T;
-    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.g.n) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.count) return;
     int x, y, z;
-    node_xyz(idx, a.g.nx, a.g.ny, x, y, z);
+    uint32_t idx;
+    if constexpr (MODE == MODE_BOX) {
+        const uint32_t zz = t / a.exy, r = t - zz * a.exy;
+        const uint32_t yy = r / a.ex;
+        x = a.lo[0] + (int)(r - yy * a.ex);
+        y = a.lo[1] + (int)yy;
+        z = a.lo[2] + (int)zz;
+        idx = ((uint32_t)z * (uint32_t)a.g.ny + (uint32_t)y) * (uint32_t)a.g.nx + (uint32_t)x;
+    } else {
+        idx = a.list[t];
+        node_xyz(idx, a.g.nx, a.g.ny, x, y, z);
+    }
     T d[LT::Q];
     pull<LT>(a.fin, a.g.stride, a.g.nx, a.g.ny, a.g.nz, x, y, z, d);
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
-    if (a.g.wallmask && any_wall(x, y, z, a.g)) wall_pass<LT, S, T, FORCE>(a.fin, a.g, idx, x, y, z, d, Fx, Fy, Fz);
+    if constexpr (MODE == MODE_LIST) wall_pass<LT, S, T, FORCE>(a.fin, a.g, idx, x, y, z, d, Fx, Fy, Fz);
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
     collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
-    static_for<LT::Q>([&](auto ic) {
-        constexpr int i = decltype(ic)::value;
-        st_dev<T>(a.fout + (unsigned long long)i * a.g.stride + idx, d[i]);
-    });
+    store_node<LT, S, T>(a.fout, a.g.stride, idx, d, a.g.sround != 0);
 }
 
 // Readout: the reference's post-stream state after the last step, from the

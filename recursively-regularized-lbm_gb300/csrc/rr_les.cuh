@@ -163,10 +163,7 @@ __global__ void __launch_bounds__(256) les_step_kernel(const LesArgs<S> a) {
             if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
             const T om1 = T(1) - T(1) / (tau + taut);
             collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Fx, Fy, Fz);
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                st_dev<T>(a.fout + (unsigned long long)i * g.stride + idx, d[i]);
-            });
+            store_node<LT, S, T>(a.fout, g.stride, idx, d, g.sround != 0);
         }
         __syncthreads();
         const int t = sm;
