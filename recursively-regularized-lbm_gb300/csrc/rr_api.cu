@@ -110,10 +110,13 @@ struct rr_solver {
     long long acc_samples = 0;
     size_t bytes = 0;
     rr::LesTile tile{32, 8, 16};
-    rr::StepRange box{};     // nodes off every wall face: launch without wall code
-    rr::StepRange shell{};   // wall-face nodes, by index list
+    int blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0}; // deep-interior box: bulk kernel
+    int bbx = 128, bby = 2;                     // its CTA shape
+    rr::StepRange shell{};   // every other node (wall faces, periodic edges), by index list
     uint32_t *shell_list = nullptr;
     int block = 256;
+    cudaStream_t side = nullptr;              // the shell launch runs beside the bulk launch
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -180,11 +183,19 @@ rr_status launch_steps(rr_solver *s, int n) {
         if (s->p.use_les) {
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
                                    s->status, s->tile, s->stream));
+        } else if (s->shell.count == 0) {
+            RR_CK(s->ops->bulk(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->blo, s->bhi,
+                               s->bbx, s->bby, s->stream));
         } else {
-            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->box,
-                               s->block, s->stream));
+            // fork: the (small, latency-bound) shell launch overlaps the bulk launch
+            RR_CK(cudaEventRecord(s->fork, s->stream));
+            RR_CK(cudaStreamWaitEvent(s->side, s->fork, 0));
             RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->shell,
-                               s->block, s->stream));
+                               s->block, s->side));
+            RR_CK(s->ops->bulk(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->blo, s->bhi,
+                               s->bbx, s->bby, s->stream));
+            RR_CK(cudaEventRecord(s->join, s->side));
+            RR_CK(cudaStreamWaitEvent(s->stream, s->join, 0));
         }
         s->cur = 1 - s->cur;
     }
@@ -295,8 +306,11 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return code;
     };
     if (set_device(s) != RR_OK) return cleanup(RR_ERR_CUDA);
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
-        return cleanup(fail(RR_ERR_CUDA, "stream creation failed"));
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess)
+        return cleanup(fail(RR_ERR_CUDA, "stream / event creation failed"));
     const size_t bytes = (size_t)p->q * g.stride * s->ops->elem_bytes;
     for (int b = 0; b < 2; b++) {
         if (cudaMalloc(&s->buf[b], bytes) != cudaSuccess) {
@@ -321,29 +335,28 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
     }
     s->bytes += 256 + sd;
-    // interior box (nodes on no wall face) and the shell list of wall-face nodes
+    // deep-interior box [1, n-1) on every axis (no upstream neighbour wraps or
+    // crosses a wall: bulk kernel) and the list of all other nodes (shell)
     {
         const int n3[3] = {p->lx, p->ly, p->lz};
-        int lo[3], ext[3];
+        bool empty = false;
         for (int a = 0; a < 3; a++) {
-            const bool wall = p->face[2 * a] != RR_FACE_PERIODIC;
-            lo[a] = wall ? 1 : 0;
-            ext[a] = wall ? n3[a] - 2 : n3[a];
-            if (ext[a] < 0) ext[a] = 0;
+            s->blo[a] = 1;
+            s->bhi[a] = n3[a] - 1;
+            if (s->bhi[a] <= s->blo[a]) empty = true;
         }
-        s->box.mode = rr::MODE_BOX;
-        s->box.count = (uint32_t)ext[0] * (uint32_t)ext[1] * (uint32_t)ext[2];
-        for (int a = 0; a < 3; a++) s->box.lo[a] = lo[a];
-        s->box.ex = (uint32_t)ext[0];
-        s->box.exy = (uint32_t)ext[0] * (uint32_t)ext[1];
-        s->box.list = nullptr;
+        if (empty)
+            for (int a = 0; a < 3; a++) s->blo[a] = s->bhi[a] = 0;
+        const int ex = s->bhi[0] - s->blo[0];
+        s->bbx = ex >= 256 ? 256 : ((ex + 31) / 32) * 32;
+        if (s->bbx < 32) s->bbx = 32;
+        s->bby = 256 / s->bbx;
         std::vector<uint32_t> shell;
-        shell.reserve(g.n - s->box.count);
         for (int z = 0; z < p->lz; z++)
             for (int y = 0; y < p->ly; y++)
                 for (int x = 0; x < p->lx; x++) {
-                    const bool in = x >= lo[0] && x < lo[0] + ext[0] && y >= lo[1] && y < lo[1] + ext[1] &&
-                                    z >= lo[2] && z < lo[2] + ext[2];
+                    const bool in = x >= s->blo[0] && x < s->bhi[0] && y >= s->blo[1] && y < s->bhi[1] &&
+                                    z >= s->blo[2] && z < s->bhi[2];
                     if (!in) shell.push_back(((uint32_t)z * p->ly + y) * p->lx + x);
                 }
         s->shell.mode = rr::MODE_LIST;
@@ -375,6 +388,7 @@ rr_status rr_destroy(rr_solver *s) {
     if (!s) return RR_OK;
     cudaSetDevice(s->p.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->side) cudaStreamSynchronize(s->side);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     cudaFree(s->buf[0]);
     cudaFree(s->buf[1]);
@@ -382,6 +396,9 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->aux);
     cudaFree(s->stat);
     cudaFree(s->shell_list);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->stream) cudaStreamDestroy(s->stream);
     cudaGetLastError();
     delete s;

@@ -33,6 +33,10 @@ struct Ops {
     cudaError_t (*step)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const StepRange &r, int block,
                         cudaStream_t st);
+    // one fused time step over the deep-interior box [lo, hi) (no wrap, no wall)
+    cudaError_t (*bulk)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
+                        const double F[3], int *status, const int lo[3], const int hi[3], int bx,
+                        int by, cudaStream_t st);
     // fused time step with the WALE eddy viscosity
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,

@@ -226,6 +226,65 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
     store_node<LT, S, T>(a.fout, a.g.stride, idx, d, a.g.sround != 0);
 }
 
+// Bulk step over the deep interior: nodes at least one node away from every
+// face, so no upstream neighbour wraps or crosses a wall.  The host passes,
+// per population, the address of population i of the upstream neighbour of
+// node 0 (fin + i*stride - (cx + cy*nx + cz*nx*ny)) and of its destination
+// (fout + i*stride); a node's loads and stores are then one multiply-add on
+// its linear index each.  The launch grid is (x blocks, y blocks, z) with no
+// integer division.  Stochastic rounding draws one hash per node and a
+// linear-congruential step per population.
+template <int Q, typename S>
+struct BulkArgs {
+    const S *src[Q];
+    S *dst[Q];
+    int lo[3], hi[3]; // box [lo, hi)
+    int nx, nxy;
+    double om1;
+    double F[3];
+    int *status;
+    int sround;
+};
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256) bulk_kernel(const BulkArgs<LT::Q, S> a) {
+    using T = typename CType<S>::T;
+    const int x = a.lo[0] + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = a.lo[1] + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int z = a.lo[2] + (int)blockIdx.z;
+    if (x >= a.hi[0] || y >= a.hi[1]) return;
+    const uint32_t idx = (uint32_t)z * (uint32_t)a.nxy + (uint32_t)y * (uint32_t)a.nx + (uint32_t)x;
+    T d[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        d[i] = ld_dev<T>(a.src[i] + idx);
+    });
+    const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    Mom<T> m = moments<LT>(d);
+    T ux, uy, uz;
+    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+    if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+        if (a.sround) {
+            // per-node seed from the node and its new state; LCG per population
+            uint32_t r = mix32(idx * 0x9E3779B9u ^ __float_as_uint(float(m.drho)) ^
+                               (__float_as_uint(float(ux)) * 0x85EBCA6Bu));
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                r = r * 1664525u + 1013904223u;
+                if constexpr (std::is_same<S, __half>::value) a.dst[i][idx] = f2h_sr(float(d[i]), r >> 19);
+                else a.dst[i][idx] = f2bf_sr(float(d[i]), r >> 16);
+            });
+            return;
+        }
+    }
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        st_dev<T>(a.dst[i] + idx, d[i]);
+    });
+}
+
 // Readout: the reference's post-stream state after the last step, from the
 // previous post-collision buffer.  Writes FP64 f (reference layout, ordering
 // given by pos: internal population i goes to output population pos[i]) and/or the

@@ -52,6 +52,7 @@ struct D3Q19 {
 
 template <typename L>
 struct Lat {
+    using Set = L; // host code indexes Set::CX etc. with run-time indices
     static constexpr int Q = L::Q;
     __host__ __device__ static constexpr int cx(int i) { return L::CX[i]; }
     __host__ __device__ static constexpr int cy(int i) { return L::CY[i]; }
