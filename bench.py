@@ -213,6 +213,11 @@ def run_gpu(args, rank, world, local_rank):
         tdist.barrier()
     torch.cuda.synchronize()
     with Clocks(local_rank) as clk:
+        # hold the stream behind a bounded spin (about 40 ms) while the host
+        # enqueues all K iterations, so host launch latency never lands
+        # inside a timed window
+        with torch.cuda.stream(stream):
+            torch.cuda._sleep(int(4e7 + 1e6 * K))
         for k in range(K):
             with torch.cuda.stream(stream):
                 flush.fill_(float(k))  # evict the populations from L2

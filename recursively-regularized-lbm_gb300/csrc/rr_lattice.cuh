@@ -16,6 +16,13 @@
 #include <type_traits>
 #include <utility>
 
+// the lattice and node arithmetic also compile as plain C++ (host checks)
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline __attribute__((always_inline))
+#endif
+
 namespace rr {
 
 template <typename F, int... I>

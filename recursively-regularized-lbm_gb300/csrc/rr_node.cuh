@@ -34,7 +34,7 @@ struct Mom {
 // zeroth, first and second moments from the deviations (macrovar.cu:4-31
 // for rho and j; the second moments feed a2neq, collision.cu:73-78)
 template <class LT, typename T>
-__device__ __forceinline__ Mom<T> moments(const T (&d)[LT::Q]) {
+__host__ __device__ __forceinline__ Mom<T> moments_generic(const T (&d)[LT::Q]) {
     Mom<T> m;
     constexpr int r = LT::rest();
     m.drho = T(LT::w(r)) * d[r];
@@ -70,7 +70,7 @@ __device__ __forceinline__ Mom<T> moments(const T (&d)[LT::Q]) {
 
 // sum_k hs(i,k) A_k : 1/2 sec_i(A)
 template <class LT, int I, typename T>
-__device__ __forceinline__ T even_poly(const T (&A)[6]) {
+__host__ __device__ __forceinline__ T even_poly(const T (&A)[6]) {
     T s = T(0);
     bool first = true;
     static_for<6>([&](auto kc) {
@@ -92,7 +92,7 @@ __device__ __forceinline__ T even_poly(const T (&A)[6]) {
 
 // 1/2 thir_i(B), plus 3 rho c.u from B[7..9] when LINEAR
 template <class LT, int I, typename T, bool LINEAR = true>
-__device__ __forceinline__ T odd_poly(const T (&B)[10]) {
+__host__ __device__ __forceinline__ T odd_poly(const T (&B)[10]) {
     // B[0..5] = b210 b201 b021 b120 b012 b102, B[6] = t111, B[7..9] = 3 rho u
     T s = T(0);
     bool first = true;
@@ -120,7 +120,7 @@ __device__ __forceinline__ T odd_poly(const T (&B)[10]) {
 // correction: sum_i H2_i f_i - rho u^ u^  (collision.cu:73-86) in the order
 // (110, 101, 011, 200, 020, 002)
 template <typename T>
-__device__ __forceinline__ void aneq_base(const Mom<T> &m, T rho, T ux, T uy, T uz, T (&n)[6]) {
+__host__ __device__ __forceinline__ void aneq_base(const Mom<T> &m, T rho, T ux, T uy, T uz, T (&n)[6]) {
     const T r3 = T(3) * rho;
     n[0] = T(3) * m.pxy - r3 * ux * uy;
     n[1] = T(3) * m.pxz - r3 * ux * uz;
@@ -133,7 +133,7 @@ __device__ __forceinline__ void aneq_base(const Mom<T> &m, T rho, T ux, T uy, T 
 // third-order coefficients (recursive a3neq, collision.cu:88-94) scaled for
 // odd_poly: b_k = (sqrt3/2) * scale * a3_k, t111 = 3 sqrt3 * scale * a111
 template <typename T>
-__device__ __forceinline__ void third_from_second(const T (&n)[6], T ux, T uy, T uz, T scale,
+__host__ __device__ __forceinline__ void third_from_second(const T (&n)[6], T ux, T uy, T uz, T scale,
                                                   T (&B)[10]) {
     const T s15 = T(1.5) * scale;
     B[0] = s15 * (n[3] * uy + T(2) * ux * n[0]); // 210
@@ -148,7 +148,7 @@ __device__ __forceinline__ void third_from_second(const T (&n)[6], T ux, T uy, T
 // equilibrium Hermite coefficients: A = rho u^ u^ (3 rho u_a u_b), b = (sqrt3/2)
 // rho u^ u^ u^ (4.5 rho u_a^2 u_b), t111 = 3 sqrt3 rho u^ v^ w^ (27 rho u v w)
 template <typename T>
-__device__ __forceinline__ void eq_coeffs(T rho, T ux, T uy, T uz, T (&A)[6], T (&B)[10]) {
+__host__ __device__ __forceinline__ void eq_coeffs(T rho, T ux, T uy, T uz, T (&A)[6], T (&B)[10]) {
     const T r3 = T(3) * rho, r45 = T(4.5) * rho;
     A[0] = r3 * ux * uy;
     A[1] = r3 * ux * uz;
@@ -171,7 +171,7 @@ __device__ __forceinline__ void eq_coeffs(T rho, T ux, T uy, T uz, T (&A)[6], T 
 // Force correction sum_i H2_ab,i Fbar_i feq_i (the f + Fbar feq term of
 // collision.cu:73-78), from the equilibrium coefficients.
 template <class LT, typename T>
-__device__ __forceinline__ void force_correction(T drho_eq, const T (&Aq)[6], const T (&Bq)[10],
+__host__ __device__ __forceinline__ void force_correction(T drho_eq, const T (&Aq)[6], const T (&Bq)[10],
                                                  T Fe, T Fx, T Fy, T Fz, T (&C)[6]) {
     constexpr int r = LT::rest();
     T Ee0 = drho_eq + even_poly<LT, r>(Aq);
@@ -206,8 +206,8 @@ __device__ __forceinline__ void force_correction(T drho_eq, const T (&Aq)[6], co
 // the first collision after a state upload takes them from the caller, as the
 // reference's first step takes init_arrays' macros, initial.cu:278-313).
 template <class LT, typename T, bool FORCE>
-__device__ __forceinline__ void collide(T (&d)[LT::Q], const Mom<T> &m, T drho_eq, T ux, T uy,
-                                        T uz, T om1, T Fx, T Fy, T Fz) {
+__host__ __device__ __forceinline__ void collide_generic(T (&d)[LT::Q], const Mom<T> &m, T drho_eq, T ux, T uy,
+                                                         T uz, T om1, T Fx, T Fy, T Fz) {
     const T rho = T(1) + drho_eq;
     T n[6];
     aneq_base(m, rho, ux, uy, uz, n);
@@ -273,9 +273,31 @@ __device__ __forceinline__ void collide(T (&d)[LT::Q], const Mom<T> &m, T drho_e
     }
 }
 
+} // namespace rr
+
+#include "rr_node27.cuh"
+
+namespace rr {
+
+// D3Q27 goes through the hand-factored forms of rr_node27.cuh (same
+// arithmetic, shared partial sums); D3Q19 and the forced collision through
+// the generic pair loop above
+template <class LT, typename T>
+__host__ __device__ __forceinline__ Mom<T> moments(const T (&d)[LT::Q]) {
+    if constexpr (LT::Q == 27) return moments27(d);
+    else return moments_generic<LT>(d);
+}
+
+template <class LT, typename T, bool FORCE>
+__host__ __device__ __forceinline__ void collide(T (&d)[LT::Q], const Mom<T> &m, T drho_eq, T ux, T uy,
+                                                 T uz, T om1, T Fx, T Fy, T Fz) {
+    if constexpr (LT::Q == 27 && !FORCE) collide27(d, m, drho_eq, ux, uy, uz, om1);
+    else collide_generic<LT, T, FORCE>(d, m, drho_eq, ux, uy, uz, om1, Fx, Fy, Fz);
+}
+
 // velocity from the moments with the half-force shift (macrovar.cu:25-28)
 template <typename T>
-__device__ __forceinline__ void velocity(const Mom<T> &m, T Fx, T Fy, T Fz, T &ux, T &uy, T &uz) {
+__host__ __device__ __forceinline__ void velocity(const Mom<T> &m, T Fx, T Fy, T Fz, T &ux, T &uy, T &uz) {
     const T inv = T(1) / (T(1) + m.drho);
     ux = (m.jx + T(0.5) * Fx) * inv;
     uy = (m.jy + T(0.5) * Fy) * inv;
@@ -286,7 +308,7 @@ __device__ __forceinline__ void velocity(const Mom<T> &m, T Fx, T Fy, T Fz, T &u
 // streaming.f90:100-140): moments of the current populations, then the
 // populations flagged in `mask` are rebuilt as feq + fneq - Fbar feq.
 template <class LT, typename T, bool FORCE>
-__device__ __forceinline__ void regularize(T (&d)[LT::Q], uint32_t mask, T Fx, T Fy, T Fz) {
+__host__ __device__ __forceinline__ void regularize(T (&d)[LT::Q], uint32_t mask, T Fx, T Fy, T Fz) {
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);

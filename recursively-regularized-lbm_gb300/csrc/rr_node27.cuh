@@ -1,0 +1,116 @@
+// rr_node27.cuh -- D3Q27 (internal order = RR27V33_code_DNS_LES/initial.cu:67-69)
+// moments and force-free RR collision with shared partial sums.
+//
+// Same quantities as moments_generic / collide_generic of rr_node.cuh; the
+// populations are grouped by class (3 axis pairs, 2 edge pairs per
+// coordinate plane, 4 corner pairs) so that the sums common to a class are
+// formed once.  Floating-point sums are not reassociated by the compiler,
+// so this factoring has to be written out.
+//
+// Population pairs (positive member / opposite):
+//   axis   1/3 (x)  2/4 (y)  5/6 (z)
+//   xy     7 (1,1,0)/9    10 (1,-1,0)/8
+//   xz     11 (1,0,1)/17  15 (1,0,-1)/13
+//   yz     12 (0,1,1)/18  16 (0,1,-1)/14
+//   corner 19 (1,1,1)/25  23 (1,1,-1)/21  22 (1,-1,1)/24  26 (1,-1,-1)/20
+#pragma once
+
+namespace rr {
+
+template <typename T>
+__host__ __device__ __forceinline__ Mom<T> moments27(const T (&d)[27]) {
+    const T w0 = T(8.0 / 27.0), w1 = T(2.0 / 27.0), w2 = T(1.0 / 54.0), w3 = T(1.0 / 216.0);
+    // axis pairs: sums s, differences g
+    const T sx = d[1] + d[3], gx = d[1] - d[3];
+    const T sy = d[2] + d[4], gy = d[2] - d[4];
+    const T sz = d[5] + d[6], gz = d[5] - d[6];
+    // edge pairs, combined per plane
+    const T s7 = d[7] + d[9], g7 = d[7] - d[9], s10 = d[10] + d[8], g10 = d[10] - d[8];
+    const T s11 = d[11] + d[17], g11 = d[11] - d[17], s15 = d[15] + d[13], g15 = d[15] - d[13];
+    const T s12 = d[12] + d[18], g12 = d[12] - d[18], s16 = d[16] + d[14], g16 = d[16] - d[14];
+    const T Sxy = s7 + s10, Dxy = s7 - s10, Jx_xy = g7 + g10, Jy_xy = g7 - g10;
+    const T Sxz = s11 + s15, Dxz = s11 - s15, Jx_xz = g11 + g15, Jz_xz = g11 - g15;
+    const T Syz = s12 + s16, Dyz = s12 - s16, Jy_yz = g12 + g16, Jz_yz = g12 - g16;
+    // corner pairs
+    const T s19 = d[19] + d[25], g19 = d[19] - d[25];
+    const T s23 = d[23] + d[21], g23 = d[23] - d[21];
+    const T s22 = d[22] + d[24], g22 = d[22] - d[24];
+    const T s26 = d[26] + d[20], g26 = d[26] - d[20];
+    const T ca = s19 + s23, cb = s22 + s26, cc = s19 - s23, ce = s22 - s26;
+    const T ga = g19 + g23, gb = g22 + g26, gc = g19 - g23, ge = g22 - g26;
+    const T Sc = ca + cb;                    // every corner
+    const T Pxy_c = ca - cb, Pxz_c = cc + ce, Pyz_c = cc - ce;
+    const T Jx_c = ga + gb, Jy_c = ga - gb, Jz_c = gc + ge;
+    Mom<T> m;
+    const T Se = Sxy + Sxz + Syz;
+    m.drho = w0 * d[0] + w1 * (sx + sy + sz) + w2 * Se + w3 * Sc;
+    m.jx = w1 * gx + w2 * (Jx_xy + Jx_xz) + w3 * Jx_c;
+    m.jy = w1 * gy + w2 * (Jy_xy + Jy_yz) + w3 * Jy_c;
+    m.jz = w1 * gz + w2 * (Jz_xz + Jz_yz) + w3 * Jz_c;
+    const T c3 = w3 * Sc;
+    m.pxx = w1 * sx + w2 * (Sxy + Sxz) + c3;
+    m.pyy = w1 * sy + w2 * (Sxy + Syz) + c3;
+    m.pzz = w1 * sz + w2 * (Sxz + Syz) + c3;
+    m.pxy = w2 * Dxy + w3 * Pxy_c;
+    m.pxz = w2 * Dxz + w3 * Pxz_c;
+    m.pyz = w2 * Dyz + w3 * Pyz_c;
+    return m;
+}
+
+// Force-free RR collision (collision.cu:41-119 with F = 0).  With A = rho a2 +
+// (1 - 1/tau) a2neq and b, t111 the merged third-order coefficients, the new
+// deviation of population i is  even_i + odd_i  with
+//   even_i = drho + 1/2 sec_i(A)
+//          = K0 + 1.5 sum_{a: c_a != 0} A_aa + 3 sum_{a<b} c_a c_b A_ab
+//   odd_i  = 3 rho c.u + 1/2 thir_i(B)
+//          = c_x X + c_y Y + c_z Z + c_x c_y c_z t111,
+//   X = 3 rho u_x + (3 c_y^2 - 1) b120 + (3 c_z^2 - 1) b102   (Y, Z likewise).
+template <typename T>
+__host__ __device__ __forceinline__ void collide27(T (&d)[27], const Mom<T> &m, T K, T ux, T uy, T uz,
+                                                   T om1) {
+    const T rho = T(1) + K;
+    T n[6];
+    aneq_base(m, rho, ux, uy, uz, n);
+    T Aq[6], Bq[10], Bn[10];
+    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
+    third_from_second(n, ux, uy, uz, om1, Bn);
+    const T A0 = Aq[0] + om1 * n[0], A1 = Aq[1] + om1 * n[1], A2 = Aq[2] + om1 * n[2];
+    const T A3 = Aq[3] + om1 * n[3], A4 = Aq[4] + om1 * n[4], A5 = Aq[5] + om1 * n[5];
+    const T b210 = Bq[0] + Bn[0], b201 = Bq[1] + Bn[1], b021 = Bq[2] + Bn[2];
+    const T b120 = Bq[3] + Bn[3], b012 = Bq[4] + Bn[4], b102 = Bq[5] + Bn[5];
+    const T t111 = Bq[6] + Bn[6];
+    // even parts
+    const T hx = T(1.5) * A3, hy = T(1.5) * A4, hz = T(1.5) * A5;
+    const T txy = T(3) * A0, txz = T(3) * A1, tyz = T(3) * A2;
+    const T K0 = K - T(0.5) * (A3 + A4 + A5);
+    const T Kx = K0 + hx, Ky = K0 + hy, Kz = K0 + hz;
+    const T Exy = Kx + hy, Exz = Kx + hz, Eyz = Ky + hz;
+    const T Ec = Exy + hz;
+    // odd parts
+    const T X00 = Bq[7] - b120 - b102, Y00 = Bq[8] - b210 - b012, Z00 = Bq[9] - b201 - b021;
+    const T X10 = X00 + T(3) * b120, X01 = X00 + T(3) * b102, X11 = X10 + T(3) * b102;
+    const T Y10 = Y00 + T(3) * b210, Y01 = Y00 + T(3) * b012, Y11 = Y10 + T(3) * b012;
+    const T Z10 = Z00 + T(3) * b201, Z01 = Z00 + T(3) * b021, Z11 = Z10 + T(3) * b021;
+    T e, o;
+    d[0] = K0;
+    d[1] = Kx + X00;
+    d[3] = Kx - X00;
+    d[2] = Ky + Y00;
+    d[4] = Ky - Y00;
+    d[5] = Kz + Z00;
+    d[6] = Kz - Z00;
+    e = Exy + txy; o = X10 + Y10; d[7] = e + o; d[9] = e - o;
+    e = Exy - txy; o = X10 - Y10; d[10] = e + o; d[8] = e - o;
+    e = Exz + txz; o = X01 + Z10; d[11] = e + o; d[17] = e - o;
+    e = Exz - txz; o = X01 - Z10; d[15] = e + o; d[13] = e - o;
+    e = Eyz + tyz; o = Y01 + Z01; d[12] = e + o; d[18] = e - o;
+    e = Eyz - tyz; o = Y01 - Z01; d[16] = e + o; d[14] = e - o;
+    const T s = txy + txz, dd = txy - txz, Ep = Ec + tyz, Em = Ec - tyz;
+    const T P = X11 + Y11, M = X11 - Y11, Qp = Z11 + t111, R = Z11 - t111;
+    e = Ep + s; o = P + Qp; d[19] = e + o; d[25] = e - o;
+    e = Em + dd; o = P - Qp; d[23] = e + o; d[21] = e - o;
+    e = Em - dd; o = M + R; d[22] = e + o; d[24] = e - o;
+    e = Ep - s; o = M - R; d[26] = e + o; d[20] = e - o;
+}
+
+} // namespace rr
