@@ -110,13 +110,9 @@ struct rr_solver {
     long long acc_samples = 0;
     size_t bytes = 0;
     rr::LesTile tile{32, 8, 16};
-    int blo[3] = {0, 0, 0}, bhi[3] = {0, 0, 0}; // deep-interior box: bulk kernel
-    int bbx = 128, bby = 2;                     // its CTA shape
-    rr::StepRange shell{};   // every other node (wall faces, periodic edges), by index list
-    uint32_t *shell_list = nullptr;
+    rr::StepRange all{};      // every node, for grids with nx < 3 (general step)
+    uint32_t *all_list = nullptr;
     int block = 256;
-    cudaStream_t side = nullptr;              // the shell launch runs beside the bulk launch
-    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -183,19 +179,11 @@ rr_status launch_steps(rr_solver *s, int n) {
         if (s->p.use_les) {
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
                                    s->status, s->tile, s->stream));
-        } else if (s->shell.count == 0) {
-            RR_CK(s->ops->bulk(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->blo, s->bhi,
-                               s->bbx, s->bby, s->stream));
+        } else if (s->p.lx >= 3) {
+            RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->stream));
         } else {
-            // fork: the (small, latency-bound) shell launch overlaps the bulk launch
-            RR_CK(cudaEventRecord(s->fork, s->stream));
-            RR_CK(cudaStreamWaitEvent(s->side, s->fork, 0));
-            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->shell,
-                               s->block, s->side));
-            RR_CK(s->ops->bulk(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->blo, s->bhi,
-                               s->bbx, s->bby, s->stream));
-            RR_CK(cudaEventRecord(s->join, s->side));
-            RR_CK(cudaStreamWaitEvent(s->stream, s->join, 0));
+            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->all,
+                               s->block, s->stream));
         }
         s->cur = 1 - s->cur;
     }
@@ -306,11 +294,8 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return code;
     };
     if (set_device(s) != RR_OK) return cleanup(RR_ERR_CUDA);
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess)
-        return cleanup(fail(RR_ERR_CUDA, "stream / event creation failed"));
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(RR_ERR_CUDA, "stream creation failed"));
     const size_t bytes = (size_t)p->q * g.stride * s->ops->elem_bytes;
     for (int b = 0; b < 2; b++) {
         if (cudaMalloc(&s->buf[b], bytes) != cudaSuccess) {
@@ -335,45 +320,22 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
     }
     s->bytes += 256 + sd;
-    // deep-interior box [1, n-1) on every axis (no upstream neighbour wraps or
-    // crosses a wall: bulk kernel) and the list of all other nodes (shell)
-    {
-        const int n3[3] = {p->lx, p->ly, p->lz};
-        bool empty = false;
-        for (int a = 0; a < 3; a++) {
-            s->blo[a] = 1;
-            s->bhi[a] = n3[a] - 1;
-            if (s->bhi[a] <= s->blo[a]) empty = true;
+    // grids thinner than 3 nodes in x run the list-driven general step over
+    // every node; all others the one-launch tile step
+    if (p->lx < 3) {
+        std::vector<uint32_t> all(g.n);
+        for (uint32_t i = 0; i < g.n; i++) all[i] = i;
+        const size_t lb = all.size() * sizeof(uint32_t);
+        if (cudaMalloc(&s->all_list, lb) != cudaSuccess) {
+            cudaGetLastError();
+            s->all_list = nullptr;
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the node list"));
         }
-        if (empty)
-            for (int a = 0; a < 3; a++) s->blo[a] = s->bhi[a] = 0;
-        const int ex = s->bhi[0] - s->blo[0];
-        s->bbx = ex >= 256 ? 256 : ((ex + 31) / 32) * 32;
-        if (s->bbx < 32) s->bbx = 32;
-        s->bby = 256 / s->bbx;
-        std::vector<uint32_t> shell;
-        for (int z = 0; z < p->lz; z++)
-            for (int y = 0; y < p->ly; y++)
-                for (int x = 0; x < p->lx; x++) {
-                    const bool in = x >= s->blo[0] && x < s->bhi[0] && y >= s->blo[1] && y < s->bhi[1] &&
-                                    z >= s->blo[2] && z < s->bhi[2];
-                    if (!in) shell.push_back(((uint32_t)z * p->ly + y) * p->lx + x);
-                }
-        s->shell.mode = rr::MODE_LIST;
-        s->shell.count = (uint32_t)shell.size();
-        s->shell.list = nullptr;
-        if (!shell.empty()) {
-            const size_t lb = shell.size() * sizeof(uint32_t);
-            if (cudaMalloc(&s->shell_list, lb) != cudaSuccess) {
-                cudaGetLastError();
-                s->shell_list = nullptr;
-                return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the wall-node list"));
-            }
-            if (cudaMemcpy(s->shell_list, shell.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
-                return cleanup(fail(RR_ERR_CUDA, "cannot upload the wall-node list"));
-            s->shell.list = s->shell_list;
-            s->bytes += lb;
-        }
+        if (cudaMemcpy(s->all_list, all.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+            return cleanup(fail(RR_ERR_CUDA, "cannot upload the node list"));
+        s->all.count = g.n;
+        s->all.list = s->all_list;
+        s->bytes += lb;
     }
     g.sround = (p->rounding == RR_ROUND_STOCHASTIC) ? 1 : 0;
     // LES tile by size class: full 32-wide rows when x allows, else 16
@@ -388,17 +350,13 @@ rr_status rr_destroy(rr_solver *s) {
     if (!s) return RR_OK;
     cudaSetDevice(s->p.device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    if (s->side) cudaStreamSynchronize(s->side);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     cudaFree(s->buf[0]);
     cudaFree(s->buf[1]);
     cudaFree(s->status);
     cudaFree(s->aux);
     cudaFree(s->stat);
-    cudaFree(s->shell_list);
-    if (s->fork) cudaEventDestroy(s->fork);
-    if (s->join) cudaEventDestroy(s->join);
-    if (s->side) cudaStreamDestroy(s->side);
+    cudaFree(s->all_list);
     if (s->stream) cudaStreamDestroy(s->stream);
     cudaGetLastError();
     delete s;

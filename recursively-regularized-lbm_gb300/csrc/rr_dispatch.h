@@ -17,13 +17,9 @@ struct LesTile {
     int tx, ty, zchunk; // tile of the WALE step kernel (autotuned per size class)
 };
 
-// nodes covered by one step launch: the box of nodes off every wall face
-// (mode 0) or the list of wall-face nodes (mode 1)
+// nodes covered by a list-driven step launch
 struct StepRange {
-    int mode;
     uint32_t count;
-    int lo[3];
-    uint32_t ex, exy;
     const uint32_t *list;
 };
 
@@ -33,10 +29,9 @@ struct Ops {
     cudaError_t (*step)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const StepRange &r, int block,
                         cudaStream_t st);
-    // one fused time step over the deep-interior box [lo, hi) (no wrap, no wall)
-    cudaError_t (*bulk)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
-                        const double F[3], int *status, const int lo[3], const int hi[3], int bx,
-                        int by, cudaStream_t st);
+    // one fused time step over the whole grid in one launch (needs nx >= 3)
+    cudaError_t (*tile)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
+                        const double F[3], int *status, cudaStream_t st);
     // fused time step with the WALE eddy viscosity
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,

@@ -175,12 +175,8 @@ __device__ __forceinline__ void wall_pass(const S *__restrict__ fin, const Geom 
     }
 }
 
-// Which nodes a step launch covers.  The nodes off every wall face form a box
-// (the whole grid for a periodic domain); a launch over that box carries no
-// wall code at all, so no warp diverges into the wall closure.  The remaining
-// wall-face nodes (the shell) go through a second launch over an index list.
-enum StepMode : int { MODE_BOX = 0, MODE_LIST = 1 };
-
+// General step over an explicit list of nodes (any node: wrap-aware pull and
+// the wall faces).  Used for grids too thin for the tile kernel (nx < 3).
 template <typename S>
 struct StepArgs {
     const S *__restrict__ fin;
@@ -190,34 +186,22 @@ struct StepArgs {
     double F[3];      // uniform body force
     int *status;      // watchdog flag (bit 0: density out of range / NaN)
     uint32_t count;   // nodes of this launch
-    int lo[3];        // MODE_BOX: first node of the box
-    uint32_t ex, exy; // MODE_BOX: box extent in x, and in x*y
-    const uint32_t *__restrict__ list; // MODE_LIST: node indices
+    const uint32_t *__restrict__ list; // node indices
 };
 
 // DNS step: one thread per node
-template <class LT, typename S, bool FORCE, int MODE>
+template <class LT, typename S, bool FORCE>
 __global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
     using T = typename CType<S>::T;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.count) return;
     int x, y, z;
-    uint32_t idx;
-    if constexpr (MODE == MODE_BOX) {
-        const uint32_t zz = t / a.exy, r = t - zz * a.exy;
-        const uint32_t yy = r / a.ex;
-        x = a.lo[0] + (int)(r - yy * a.ex);
-        y = a.lo[1] + (int)yy;
-        z = a.lo[2] + (int)zz;
-        idx = ((uint32_t)z * (uint32_t)a.g.ny + (uint32_t)y) * (uint32_t)a.g.nx + (uint32_t)x;
-    } else {
-        idx = a.list[t];
-        node_xyz(idx, a.g.nx, a.g.ny, x, y, z);
-    }
+    const uint32_t idx = a.list[t];
+    node_xyz(idx, a.g.nx, a.g.ny, x, y, z);
     T d[LT::Q];
     pull<LT>(a.fin, a.g.stride, a.g.nx, a.g.ny, a.g.nz, x, y, z, d);
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
-    if constexpr (MODE == MODE_LIST) wall_pass<LT, S, T, FORCE>(a.fin, a.g, idx, x, y, z, d, Fx, Fy, Fz);
+    if (a.g.wallmask && any_wall(x, y, z, a.g)) wall_pass<LT, S, T, FORCE>(a.fin, a.g, idx, x, y, z, d, Fx, Fy, Fz);
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
@@ -226,48 +210,110 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
     store_node<LT, S, T>(a.fout, a.g.stride, idx, d, a.g.sround != 0);
 }
 
-// Bulk step over the deep interior: nodes at least one node away from every
-// face, so no upstream neighbour wraps or crosses a wall.  The host passes,
-// per population, the address of population i of the upstream neighbour of
-// node 0 (fin + i*stride - (cx + cy*nx + cz*nx*ny)) and of its destination
-// (fout + i*stride); a node's loads and stores are then one multiply-add on
-// its linear index each.  The launch grid is (x blocks, y blocks, z) with no
-// integer division.  Stochastic rounding draws one hash per node and a
-// linear-congruential step per population.
+// Division by a run-time constant d < 2^31 for numerators n < 2^31:
+// q = (umulhi(n, m) + n) >> s with s = ceil(log2 d), m = 2^32 (2^s - d) / d + 1.
+struct FastDiv {
+    uint32_t d, m, s;
+};
+__host__ inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t s = 0;
+    while ((1ull << s) < d) s++;
+    const unsigned long long m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, s};
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return (__umulhi(n, f.m) + n) >> f.s;
+}
+
+// One-launch step with warp-granular work items.  The grid's warps walk
+// groups of ROWS_PER_ITEM_GROUP x-rows (row = z*ny + y).  A group holds, per
+// row, ceil((nx-2)/32) items of 32 consecutive nodes over x in [1, nx-2], and
+// one last item with the 2 x-face nodes (x = 0 and x = nx-1) of each of its
+// rows.  The x-face nodes are therefore processed in the same window as
+// their rows (the data they need sits in L2), and every item is uniform over
+// its warp: rows off every y/z face take the fast path (no wrap, no wall,
+// precomputed population addresses), wall / periodic-edge rows and x-face
+// items take the general path (wrap-aware pull + wall faces), compiled
+// out of line so that it does not raise the fast path's register count.
+constexpr int ROWS_PER_ITEM_GROUP = 16;
+
 template <int Q, typename S>
-struct BulkArgs {
-    const S *src[Q];
-    S *dst[Q];
-    int lo[3], hi[3]; // box [lo, hi)
-    int nx, nxy;
+struct TileArgs {
+    const S *src[Q]; // fast path: upstream-neighbour address of node 0, per population
+    S *dst[Q];       // destination of node 0, per population
+    const S *fin;
+    Geom g;
+    uint32_t nitems, nrows, segs, group_items;
+    FastDiv div_group, div_segs, div_ny;
     double om1;
     double F[3];
     int *status;
-    int sround;
 };
 
-template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256) bulk_kernel(const BulkArgs<LT::Q, S> a) {
-    using T = typename CType<S>::T;
-    const int x = a.lo[0] + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int y = a.lo[1] + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    const int z = a.lo[2] + (int)blockIdx.z;
-    if (x >= a.hi[0] || y >= a.hi[1]) return;
-    const uint32_t idx = (uint32_t)z * (uint32_t)a.nxy + (uint32_t)y * (uint32_t)a.nx + (uint32_t)x;
+template <class LT, typename S, typename T, bool FORCE>
+__device__ __noinline__ void general_node(const S *__restrict__ fin, const Geom &g, uint32_t idx, int x, int y,
+                                          int z, T Fx, T Fy, T Fz, T *out) {
     T d[LT::Q];
+    pull<LT>(fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+    if (g.wallmask && any_wall(x, y, z, g)) wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        d[i] = ld_dev<T>(a.src[i] + idx);
+        out[i] = d[i];
     });
+}
+
+template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const TileArgs<LT::Q, S> a) {
+    using T = typename CType<S>::T;
+    const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (item >= a.nitems) return;
+    const Geom &g = a.g;
+    const uint32_t grp = fdiv(item, a.div_group);
+    const uint32_t sub = item - grp * a.group_items;
+    uint32_t row;
+    int x;
+    bool fast;
+    if (sub < ROWS_PER_ITEM_GROUP * a.segs) {
+        const uint32_t rl = fdiv(sub, a.div_segs);
+        row = grp * ROWS_PER_ITEM_GROUP + rl;
+        x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
+        fast = true;
+        if (x > g.nx - 2) return;
+    } else {
+        row = grp * ROWS_PER_ITEM_GROUP + (lane >> 1);
+        x = (lane & 1u) ? g.nx - 1 : 0;
+        fast = false;
+    }
+    if (row >= a.nrows) return;
+    const int z = (int)fdiv(row, a.div_ny);
+    const int y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+    fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
+    const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    T d[LT::Q];
+    if (fast) {
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            d[i] = ld_dev<T>(a.src[i] + idx);
+        });
+    } else {
+        T tmp[LT::Q];
+        general_node<LT, S, T, FORCE>(a.fin, g, idx, x, y, z, Fx, Fy, Fz, tmp);
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            d[i] = tmp[i];
+        });
+    }
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
     collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
-        if (a.sround) {
-            // per-node seed from the node and its new state; LCG per population
+        if (g.sround) {
             uint32_t r = mix32(idx * 0x9E3779B9u ^ __float_as_uint(float(m.drho)) ^
                                (__float_as_uint(float(ux)) * 0x85EBCA6Bu));
             static_for<LT::Q>([&](auto ic) {

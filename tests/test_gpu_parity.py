@@ -100,6 +100,16 @@ def test_les_partial_tiles_and_forcing_axes():
     _check(_run_pair(p, st, [1, 12]), st["uc"])
 
 
+@pytest.mark.parametrize("dims", [(34, 7, 5), (2, 9, 6), (3, 3, 3), (67, 5, 4)])
+def test_odd_grids(dims):
+    # x-rows whose interior is a multiple of the warp width, row counts that
+    # are not a multiple of the row group, the thin-grid fallback (nx < 3)
+    nx, ny, nz = dims
+    p, st = presets.channel(nx=nx, ny=ny, nz=nz, les=False, variant="config", amp=0.3)
+    p.force[1] = 3e-6
+    _check(_run_pair(p, st, [1, 9]), st["uc"])
+
+
 def test_fortran_order_readout():
     p, st = presets.cavity(n=10, Re=50.0, U=0.1, variant="config")
     with rrlbm.Solver(p) as s:
