@@ -15,7 +15,7 @@
 #include <sys/stat.h>
 #include <vector>
 
-#include "../../include/rr_api.h"
+#include "rr_api.h"
 #include "rr_aux.h"
 #include "rr_dispatch.h"
 #include "rr_kernels.cuh"

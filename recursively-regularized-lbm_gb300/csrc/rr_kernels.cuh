@@ -228,14 +228,14 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
 // One-launch step with warp-granular work items.  The grid's warps walk
 // groups of ROWS_PER_ITEM_GROUP x-rows (row = z*ny + y).  A group holds, per
 // row, ceil((nx-2)/32) items of 32 consecutive nodes over x in [1, nx-2], and
-// one last item with the 2 x-face nodes (x = 0 and x = nx-1) of each of its
-// rows.  The x-face nodes are therefore processed in the same window as
-// their rows (the data they need sits in L2), and every item is uniform over
-// its warp: rows off every y/z face take the fast path (no wrap, no wall,
-// precomputed population addresses), wall / periodic-edge rows and x-face
-// items take the general path (wrap-aware pull + wall faces), compiled
-// out of line so that it does not raise the fast path's register count.
-constexpr int ROWS_PER_ITEM_GROUP = 16;
+// two last items with the x = 0 and the x = nx-1 nodes of its 32 rows.  The
+// x-face nodes are therefore processed in the same window as their rows (the
+// data they need sits in L2), and every item is uniform over its warp: rows
+// off every y/z face take the fast path (no wrap, no wall, precomputed
+// population addresses); wall / periodic-edge rows and x-face items take the
+// wrap-aware pull and, per node, the closure of its wall face compiled for
+// that face (edge and corner nodes: the general face loop, out of line).
+constexpr int ROWS_PER_ITEM_GROUP = 32;
 
 template <int Q, typename S>
 struct TileArgs {
@@ -250,15 +250,49 @@ struct TileArgs {
     int *status;
 };
 
-template <class LT, typename S, typename T, bool FORCE>
-__device__ __noinline__ void general_node(const S *__restrict__ fin, const Geom &g, uint32_t idx, int x, int y,
-                                          int z, T Fx, T Fy, T Fz, T *out) {
-    T d[LT::Q];
-    pull<LT>(fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
-    if (g.wallmask && any_wall(x, y, z, g)) wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
+// populations entering the domain through face F (0..5 = x-lo .. z-hi)
+template <class LT, int F>
+__host__ __device__ constexpr uint32_t entering_mask() {
+    uint32_t m = 0;
+    for (int i = 0; i < LT::Q; i++) {
+        const int c = F / 2 == 0 ? LT::cx(i) : (F / 2 == 1 ? LT::cy(i) : LT::cz(i));
+        if ((F & 1) ? c < 0 : c > 0) m |= 1u << i;
+    }
+    return m;
+}
+
+// one wall face known at compile time: bounce-back + regularized closure of
+// its entering populations only
+template <class LT, typename S, typename T, bool FORCE, int F>
+__device__ __forceinline__ void wall_face(const S *__restrict__ fin, const Geom &g, uint32_t idx, T (&d)[LT::Q],
+                                          T Fx, T Fy, T Fz) {
+    constexpr uint32_t M = entering_mask<LT, F>();
+    const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        out[i] = d[i];
+        if constexpr (((M >> i) & 1u) != 0) {
+            constexpr int o = LT::opp(i);
+            const T v = ld_dev<T>(fin + (unsigned long long)o * g.stride + idx);
+            d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+        }
+    });
+    if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
+}
+
+// nodes on two or three wall faces (edges and corners of a walled box): the
+// face loop in the reference order, out of line (rare)
+template <class LT, typename S, typename T, bool FORCE>
+__device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g, uint32_t idx, int x, int y,
+                                        int z, T Fx, T Fy, T Fz, T *dd) {
+    T d[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        d[i] = dd[i];
+    });
+    wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        dd[i] = d[i];
     });
 }
 
@@ -283,8 +317,9 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
         fast = true;
         if (x > g.nx - 2) return;
     } else {
-        row = grp * ROWS_PER_ITEM_GROUP + (lane >> 1);
-        x = (lane & 1u) ? g.nx - 1 : 0;
+        // the x = 0 (first) or x = nx-1 (second) nodes of the group's rows
+        row = grp * ROWS_PER_ITEM_GROUP + lane;
+        x = (sub == ROWS_PER_ITEM_GROUP * a.segs) ? 0 : g.nx - 1;
         fast = false;
     }
     if (row >= a.nrows) return;
@@ -300,12 +335,33 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
             d[i] = ld_dev<T>(a.src[i] + idx);
         });
     } else {
-        T tmp[LT::Q];
-        general_node<LT, S, T, FORCE>(a.fin, g, idx, x, y, z, Fx, Fy, Fz, tmp);
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            d[i] = tmp[i];
-        });
+        pull<LT>(a.fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+        const uint32_t faces = g.wallmask & ((x == 0 ? 1u : 0u) | (x == g.nx - 1 ? 2u : 0u) | (y == 0 ? 4u : 0u) |
+                                             (y == g.ny - 1 ? 8u : 0u) | (z == 0 ? 16u : 0u) |
+                                             (z == g.nz - 1 ? 32u : 0u));
+        if (faces != 0u) {
+            if ((faces & (faces - 1u)) == 0u) {
+                switch (__ffs(faces) - 1) {
+                case 0: wall_face<LT, S, T, FORCE, 0>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 1: wall_face<LT, S, T, FORCE, 1>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 2: wall_face<LT, S, T, FORCE, 2>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 3: wall_face<LT, S, T, FORCE, 3>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 4: wall_face<LT, S, T, FORCE, 4>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                default: wall_face<LT, S, T, FORCE, 5>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                }
+            } else {
+                T tmp[LT::Q];
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    tmp[i] = d[i];
+                });
+                wall_multi<LT, S, T, FORCE>(a.fin, g, idx, x, y, z, Fx, Fy, Fz, tmp);
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    d[i] = tmp[i];
+                });
+            }
+        }
     }
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;

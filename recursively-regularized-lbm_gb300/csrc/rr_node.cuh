@@ -307,7 +307,9 @@ __host__ __device__ __forceinline__ void velocity(const Mom<T> &m, T Fx, T Fy, T
 // Regularized wall closure of one node (RRBC, BC.cu:4-126; Cavity
 // streaming.f90:100-140): moments of the current populations, then the
 // populations flagged in `mask` are rebuilt as feq + fneq - Fbar feq.
-template <class LT, typename T, bool FORCE>
+// CMASK is a compile-time superset of `mask` (the entering set of a face
+// known at compile time): populations outside it generate no code.
+template <class LT, typename T, bool FORCE, uint32_t CMASK = 0xFFFFFFFFu>
 __host__ __device__ __forceinline__ void regularize(T (&d)[LT::Q], uint32_t mask, T Fx, T Fy, T Fz) {
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
@@ -329,6 +331,7 @@ __host__ __device__ __forceinline__ void regularize(T (&d)[LT::Q], uint32_t mask
     third_from_second(n, ux, uy, uz, T(1), Bn);
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
+        if constexpr (((CMASK >> i) & 1u) != 0)
         if ((mask >> i) & 1u) {
             T Ee = m.drho + even_poly<LT, i>(Aq);
             T Eo = odd_poly<LT, i>(Bq);
