@@ -112,6 +112,8 @@ struct rr_solver {
     rr::LesTile tile{32, 8, 16};
     rr::StepRange all{};      // every node, for grids with nx < 3 (general step)
     uint32_t *all_list = nullptr;
+    uint32_t *edge_list = nullptr; // x-end nodes of rows on a y/z wall (tile step)
+    uint32_t nedges = 0;
     int block = 256;
     cudaGraphExec_t graph = nullptr;
 };
@@ -180,7 +182,8 @@ rr_status launch_steps(rr_solver *s, int n) {
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
                                    s->status, s->tile, s->stream));
         } else if (s->p.lx >= 3) {
-            RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->stream));
+            RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->edge_list,
+                               s->nedges, s->stream));
         } else {
             RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->all,
                                s->block, s->stream));
@@ -320,6 +323,34 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
     }
     s->bytes += 256 + sd;
+    // the tile step's edge nodes: x = 0 and x = nx-1 of every row lying on a
+    // y or z wall face
+    if (p->lx >= 3) {
+        std::vector<uint32_t> edges;
+        for (int z = 0; z < p->lz; z++)
+            for (int y = 0; y < p->ly; y++) {
+                const bool yzw = (p->face[2] != RR_FACE_PERIODIC && y == 0) ||
+                                 (p->face[3] != RR_FACE_PERIODIC && y == p->ly - 1) ||
+                                 (p->face[4] != RR_FACE_PERIODIC && z == 0) ||
+                                 (p->face[5] != RR_FACE_PERIODIC && z == p->lz - 1);
+                if (!yzw) continue;
+                const uint32_t row = (uint32_t)z * p->ly + y;
+                edges.push_back(row * p->lx);
+                edges.push_back(row * p->lx + p->lx - 1);
+            }
+        if (!edges.empty()) {
+            const size_t lb = edges.size() * sizeof(uint32_t);
+            if (cudaMalloc(&s->edge_list, lb) != cudaSuccess) {
+                cudaGetLastError();
+                s->edge_list = nullptr;
+                return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the edge-node list"));
+            }
+            if (cudaMemcpy(s->edge_list, edges.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+                return cleanup(fail(RR_ERR_CUDA, "cannot upload the edge-node list"));
+            s->nedges = (uint32_t)edges.size();
+            s->bytes += lb;
+        }
+    }
     // grids thinner than 3 nodes in x run the list-driven general step over
     // every node; all others the one-launch tile step
     if (p->lx < 3) {
@@ -357,6 +388,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->aux);
     cudaFree(s->stat);
     cudaFree(s->all_list);
+    cudaFree(s->edge_list);
     if (s->stream) cudaStreamDestroy(s->stream);
     cudaGetLastError();
     delete s;

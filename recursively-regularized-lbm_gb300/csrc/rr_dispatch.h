@@ -29,9 +29,11 @@ struct Ops {
     cudaError_t (*step)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const StepRange &r, int block,
                         cudaStream_t st);
-    // one fused time step over the whole grid in one launch (needs nx >= 3)
+    // one fused time step over the whole grid in one launch (needs nx >= 3);
+    // edges: the x-end nodes of rows on a y/z wall face
     cudaError_t (*tile)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
-                        const double F[3], int *status, cudaStream_t st);
+                        const double F[3], int *status, const uint32_t *edges, uint32_t nedges,
+                        cudaStream_t st);
     // fused time step with the WALE eddy viscosity
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,

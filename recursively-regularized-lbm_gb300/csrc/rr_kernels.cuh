@@ -244,7 +244,11 @@ struct TileArgs {
     const S *fin;
     Geom g;
     uint32_t nitems, nrows, segs, group_items;
-    FastDiv div_group, div_segs, div_ny;
+    uint32_t nmain;                  // items of the row groups; the rest are edge items
+    const uint32_t *edges;           // x-end nodes of rows on a y/z wall face
+    uint32_t nedges;
+    uint32_t yzwall;                 // bit 0: y-lo, 1: y-hi, 2: z-lo, 3: z-hi walls
+    FastDiv div_group, div_segs, div_ny, div_nx;
     double om1;
     double F[3];
     int *status;
@@ -305,27 +309,43 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
     const uint32_t lane = threadIdx.x & 31u;
     if (item >= a.nitems) return;
     const Geom &g = a.g;
-    const uint32_t grp = fdiv(item, a.div_group);
-    const uint32_t sub = item - grp * a.group_items;
     uint32_t row;
-    int x;
+    int x, y, z;
     bool fast;
-    if (sub < ROWS_PER_ITEM_GROUP * a.segs) {
-        const uint32_t rl = fdiv(sub, a.div_segs);
-        row = grp * ROWS_PER_ITEM_GROUP + rl;
-        x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
-        fast = true;
-        if (x > g.nx - 2) return;
+    if (item < a.nmain) {
+        const uint32_t grp = fdiv(item, a.div_group);
+        const uint32_t sub = item - grp * a.group_items;
+        bool xface = false;
+        if (sub < ROWS_PER_ITEM_GROUP * a.segs) {
+            const uint32_t rl = fdiv(sub, a.div_segs);
+            row = grp * ROWS_PER_ITEM_GROUP + rl;
+            x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
+            fast = true;
+            if (x > g.nx - 2) return;
+        } else {
+            // the x = 0 (first) or x = nx-1 (second) nodes of the group's rows
+            row = grp * ROWS_PER_ITEM_GROUP + lane;
+            x = (sub == ROWS_PER_ITEM_GROUP * a.segs) ? 0 : g.nx - 1;
+            fast = false;
+            xface = true;
+        }
+        if (row >= a.nrows) return;
+        z = (int)fdiv(row, a.div_ny);
+        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+        const bool yzw = ((a.yzwall & 1u) && y == 0) || ((a.yzwall & 2u) && y == g.ny - 1) ||
+                         ((a.yzwall & 4u) && z == 0) || ((a.yzwall & 8u) && z == g.nz - 1);
+        if (xface && yzw) return; // an edge node: handled by the edge items
+        fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
     } else {
-        // the x = 0 (first) or x = nx-1 (second) nodes of the group's rows
-        row = grp * ROWS_PER_ITEM_GROUP + lane;
-        x = (sub == ROWS_PER_ITEM_GROUP * a.segs) ? 0 : g.nx - 1;
+        const uint32_t e = (item - a.nmain) * 32u + lane;
+        if (e >= a.nedges) return;
+        const uint32_t nidx = a.edges[e];
+        row = fdiv(nidx, a.div_nx);
+        x = (int)(nidx - row * (uint32_t)g.nx);
+        z = (int)fdiv(row, a.div_ny);
+        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
         fast = false;
     }
-    if (row >= a.nrows) return;
-    const int z = (int)fdiv(row, a.div_ny);
-    const int y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
-    fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
     const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
     T d[LT::Q];
