@@ -248,6 +248,7 @@ struct TileArgs {
     const uint32_t *edges;           // x-end nodes of rows on a y/z wall face
     uint32_t nedges;
     uint32_t yzwall;                 // bit 0: y-lo, 1: y-hi, 2: z-lo, 3: z-hi walls
+    uint32_t rot;                    // row rotation: (nz-1)*ny puts the last z plane first
     FastDiv div_group, div_segs, div_ny, div_nx;
     double om1;
     double F[3];
@@ -312,9 +313,14 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
     uint32_t row;
     int x, y, z;
     bool fast;
-    if (item < a.nmain) {
-        const uint32_t grp = fdiv(item, a.div_group);
-        const uint32_t sub = item - grp * a.group_items;
+    // the slow items go first so that they overlap the bulk instead of
+    // forming a tail: the edge items, then the rows of the last z plane (the
+    // row order is rotated by one plane)
+    const uint32_t nedge_items = a.nitems - a.nmain;
+    if (item >= nedge_items) {
+        const uint32_t mitem = item - nedge_items;
+        const uint32_t grp = fdiv(mitem, a.div_group);
+        const uint32_t sub = mitem - grp * a.group_items;
         bool xface = false;
         if (sub < ROWS_PER_ITEM_GROUP * a.segs) {
             const uint32_t rl = fdiv(sub, a.div_segs);
@@ -330,6 +336,8 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
             xface = true;
         }
         if (row >= a.nrows) return;
+        row += a.rot;
+        if (row >= a.nrows) row -= a.nrows;
         z = (int)fdiv(row, a.div_ny);
         y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
         const bool yzw = ((a.yzwall & 1u) && y == 0) || ((a.yzwall & 2u) && y == g.ny - 1) ||
@@ -337,7 +345,7 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
         if (xface && yzw) return; // an edge node: handled by the edge items
         fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
     } else {
-        const uint32_t e = (item - a.nmain) * 32u + lane;
+        const uint32_t e = item * 32u + lane;
         if (e >= a.nedges) return;
         const uint32_t nidx = a.edges[e];
         row = fdiv(nidx, a.div_nx);
