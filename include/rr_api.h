@@ -135,6 +135,21 @@ rr_status rr_get_f(rr_solver *s, double *f, int where);
 /* diag_flow's statistics (output.cu:24-35): {umean, vmean, wmean, rhomean} */
 rr_status rr_diag(rr_solver *s, double out[4]);
 
+/* The same four means of FP64 fields that already live on the device (n
+ * values each), written to the device array out[4] on `stream` (a
+ * cudaStream_t, NULL for the default stream), without allocating anything.
+ * No counterpart in the reference.  It is for callers that may not allocate
+ * device memory when they ask for the statistics: a server whose HBM budget
+ * is fully handed out to resident domains, or a latency-critical loop that
+ * cannot afford a cudaMalloc.  The partial sums use a fixed 32 KiB array that
+ * every GPU loading the library holds until the process exits; n must be 1 to
+ * 2147483647.  The first call on a device looks up that array's device
+ * address (with the device current), so make it before any stream capture.
+ * Calls share the array: two calls that overlap on the GPU race.  Nothing is
+ * synchronised; read out[] after the stream's work completes. */
+rr_status rr_diag_fields_noalloc(const double *rho, const double *ux, const double *uy,
+                                 const double *uz, size_t n, double *out, void *stream);
+
 /* output_profile's statistics per y plane (output.cu:181-214), FP64 on the
  * device: out[iy * 11 + k] for k = y+0.5, (y+0.5)/ystar, <u>, <v>, <w>,
  * <u'u'>, <v'v'>, <w'w'>, <u'v'>, <u'w'>, <v'w'>, and out[LY*11 + iy] = <tau_t>

@@ -233,6 +233,17 @@ rr_status ensure_dir(const char *dir) {
 
 } // namespace
 
+// sets this thread's rr_last_error() text for entry points in other files
+rr_status rr_internal_error(rr_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
 extern "C" {
 
 const char *rr_last_error(void) { return g_err.c_str(); }

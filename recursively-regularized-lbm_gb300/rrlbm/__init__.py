@@ -74,6 +74,7 @@ def lib():
             "rr_macro": ([vp, vp, vp, vp, vp, vp, ctypes.c_int], ctypes.c_int),
             "rr_get_f": ([vp, vp, ctypes.c_int], ctypes.c_int),
             "rr_diag": ([vp, dp], ctypes.c_int),
+            "rr_diag_fields_noalloc": ([vp, vp, vp, vp, ctypes.c_size_t, vp, vp], ctypes.c_int),
             "rr_profile": ([vp, dp], ctypes.c_int),
             "rr_accumulate": ([vp], ctypes.c_int),
             "rr_get_accum": ([vp, dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
