@@ -66,7 +66,7 @@ def peaks():
 
 def ncu_traffic(wl):
     """DRAM bytes per step-kernel launch from the committed ncu summary, if any"""
-    path = os.path.join(ROOT, "profiles", f"step_kernel_{wl}.txt")
+    path = os.path.join(ROOT, "profiles", f"tile_kernel_{wl}.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):

@@ -228,14 +228,17 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
 // One-launch step with warp-granular work items.  The grid's warps walk
 // groups of ROWS_PER_ITEM_GROUP x-rows (row = z*ny + y).  A group holds, per
 // row, ceil((nx-2)/32) items of 32 consecutive nodes over x in [1, nx-2], and
-// two last items with the x = 0 and the x = nx-1 nodes of its 32 rows.  The
-// x-face nodes are therefore processed in the same window as their rows (the
-// data they need sits in L2), and every item is uniform over its warp: rows
-// off every y/z face take the fast path (no wrap, no wall, precomputed
-// population addresses); wall / periodic-edge rows and x-face items take the
-// wrap-aware pull and, per node, the closure of its wall face compiled for
-// that face (edge and corner nodes: the general face loop, out of line).
-constexpr int ROWS_PER_ITEM_GROUP = 32;
+// then XFACE_ITEMS items with the x = 0 and the x = nx-1 nodes of its rows,
+// 32 rows per item.  The x-face nodes are therefore processed in the same
+// window as their rows (the data they need sits in L2), they fill whole CTAs
+// of their own (a slow warp does not hold a CTA of fast ones resident), and
+// every item is uniform over its warp: rows off every y/z face take the fast
+// path (no wrap, no wall, precomputed population addresses); wall /
+// periodic-edge rows and x-face items take the wrap-aware pull and, per node,
+// the closure of its wall face compiled for that face (edge and corner
+// nodes: the general face loop, out of line).
+constexpr int ROWS_PER_ITEM_GROUP = 256;
+constexpr int XFACE_ITEMS = 2 * ROWS_PER_ITEM_GROUP / 32; // x = 0 items, then x = nx-1 items
 
 template <int Q, typename S>
 struct TileArgs {
@@ -329,9 +332,12 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
             fast = true;
             if (x > g.nx - 2) return;
         } else {
-            // the x = 0 (first) or x = nx-1 (second) nodes of the group's rows
-            row = grp * ROWS_PER_ITEM_GROUP + lane;
-            x = (sub == ROWS_PER_ITEM_GROUP * a.segs) ? 0 : g.nx - 1;
+            // the x = 0 nodes of the group's rows, 32 per item, then the
+            // x = nx-1 nodes: whole CTAs of these slower items
+            const uint32_t xi = sub - ROWS_PER_ITEM_GROUP * a.segs;
+            const uint32_t half = XFACE_ITEMS / 2;
+            row = grp * ROWS_PER_ITEM_GROUP + (xi % half) * 32u + lane;
+            x = xi < half ? 0 : g.nx - 1;
             fast = false;
             xface = true;
         }
