@@ -237,7 +237,7 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
 // periodic-edge rows and x-face items take the wrap-aware pull and, per node,
 // the closure of its wall face compiled for that face (edge and corner
 // nodes: the general face loop, out of line).
-constexpr int ROWS_PER_ITEM_GROUP = 256;
+constexpr int ROWS_PER_ITEM_GROUP = 32;
 constexpr int XFACE_ITEMS = 2 * ROWS_PER_ITEM_GROUP / 32; // x = 0 items, then x = nx-1 items
 
 template <int Q, typename S>
@@ -287,6 +287,29 @@ __device__ __forceinline__ void wall_face(const S *__restrict__ fin, const Geom 
     if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
 }
 
+// A node on exactly one wall face F and at least one node away from every
+// other face: its populations that do not enter through F come from inside
+// the domain (no wrap), so they use the fast path's precomputed addresses;
+// the entering ones are bounced back from this node's own post-collision
+// populations.  Then the regularized closure of the entering set.
+template <class LT, typename S, typename T, bool FORCE, int F>
+__device__ __forceinline__ void wall_fast(const S *const *src, const S *__restrict__ fin, const Geom &g,
+                                          uint32_t idx, T (&d)[LT::Q], T Fx, T Fy, T Fz) {
+    constexpr uint32_t M = entering_mask<LT, F>();
+    const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        if constexpr (((M >> i) & 1u) != 0) {
+            constexpr int o = LT::opp(i);
+            const T v = ld_dev<T>(fin + (unsigned long long)o * g.stride + idx);
+            d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+        } else {
+            d[i] = ld_dev<T>(src[i] + idx);
+        }
+    });
+    if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
+}
+
 // nodes on two or three wall faces (edges and corners of a walled box): the
 // face loop in the reference order, out of line (rare)
 template <class LT, typename S, typename T, bool FORCE>
@@ -307,7 +330,7 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
 
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const TileArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
@@ -369,11 +392,26 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const T
             d[i] = ld_dev<T>(a.src[i] + idx);
         });
     } else {
-        pull<LT>(a.fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+        const bool xi = x >= 1 && x <= g.nx - 2, yi = y >= 1 && y <= g.ny - 2, zi = z >= 1 && z <= g.nz - 2;
         const uint32_t faces = g.wallmask & ((x == 0 ? 1u : 0u) | (x == g.nx - 1 ? 2u : 0u) | (y == 0 ? 4u : 0u) |
                                              (y == g.ny - 1 ? 8u : 0u) | (z == 0 ? 16u : 0u) |
                                              (z == g.nz - 1 ? 32u : 0u));
-        if (faces != 0u) {
+        // one wall face, interior on the other two axes
+        int wf = -1;
+        if (faces == 1u || faces == 2u) wf = (yi && zi) ? (faces == 1u ? 0 : 1) : -1;
+        else if (faces == 4u || faces == 8u) wf = (xi && zi) ? (faces == 4u ? 2 : 3) : -1;
+        else if (faces == 16u || faces == 32u) wf = (xi && yi) ? (faces == 16u ? 4 : 5) : -1;
+        switch (wf) {
+        case 0: wall_fast<LT, S, T, FORCE, 0>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        case 1: wall_fast<LT, S, T, FORCE, 1>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        case 2: wall_fast<LT, S, T, FORCE, 2>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        case 3: wall_fast<LT, S, T, FORCE, 3>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        case 4: wall_fast<LT, S, T, FORCE, 4>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        case 5: wall_fast<LT, S, T, FORCE, 5>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+        default: break;
+        }
+        if (wf < 0) pull<LT>(a.fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+        if (wf < 0 && faces != 0u) {
             if ((faces & (faces - 1u)) == 0u) {
                 switch (__ffs(faces) - 1) {
                 case 0: wall_face<LT, S, T, FORCE, 0>(a.fin, g, idx, d, Fx, Fy, Fz); break;
