@@ -68,38 +68,63 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     return x;
 }
 
-// Stochastic rounding to 16 bits: r is added to the float bits that the
-// conversion drops (13 for FP16, 16 for BF16) before truncating, so the
-// magnitude is rounded up with probability (dropped fraction) / 2^bits and the
-// stored value is unbiased.  Round-to-nearest stalls a slowly varying field
-// whose per-step change is below half a unit in the last place (e.g. the
-// Ma = 0.01 Taylor-Green decay); unbiased rounding keeps that change in
-// expectation.  For FP16 subnormals the rounding is biased toward zero by less
-// than one subnormal step (6e-8).
-__device__ __forceinline__ __half f2h_sr(float v, uint32_t r) {
-    return __float2half_rz(__uint_as_float(__float_as_uint(v) + (r & 0x1FFFu)));
+// Stochastic rounding to 16 bits rounds a value up in magnitude with
+// probability (dropped fraction) / (unit in the last place), so the stored
+// value is unbiased.  Round-to-nearest stalls a slowly varying field whose
+// per-step change is below half a unit in the last place (e.g. the Ma = 0.01
+// Taylor-Green decay); unbiased rounding keeps that change in expectation.
+// Two FP32 values to a 16-bit pair with the hardware's stochastic rounding
+// (cvt.rs, sm_100-family): hi goes to bits 31:16, lo to bits 15:0, rbits
+// supplies the random bits.
+template <typename S>
+__device__ __forceinline__ uint32_t cvt_sr2(float hi, float lo, uint32_t rbits) {
+    uint32_t h2;
+    if constexpr (std::is_same<S, __half>::value)
+        asm("cvt.rs.satfinite.f16x2.f32 %0, %1, %2, %3;" : "=r"(h2) : "f"(hi), "f"(lo), "r"(rbits));
+    else
+        asm("cvt.rs.satfinite.bf16x2.f32 %0, %1, %2, %3;" : "=r"(h2) : "f"(hi), "f"(lo), "r"(rbits));
+    return h2;
 }
-__device__ __forceinline__ __nv_bfloat16 f2bf_sr(float v, uint32_t r) {
-    return __float2bfloat16_rz(__uint_as_float(__float_as_uint(v) + (r & 0xFFFFu)));
+
+// Stochastic-rounding store of one node's populations to FP16/BF16, two
+// populations per conversion.  The random bits: one hash of the node seeds a
+// linear-congruential stream, one 32-bit draw per pair, folded as
+// r ^ (r >> 16) so that both halves carry high-order LCG bits.  at(i) is the
+// address of population i.
+template <class LT, typename S, typename T, class Addr>
+__device__ __forceinline__ void store_sr_pairs(const T (&d)[LT::Q], uint32_t seed, Addr at) {
+    uint32_t r = seed;
+    static_for<(LT::Q + 1) / 2>([&](auto jc) {
+        constexpr int i0 = 2 * decltype(jc)::value, i1 = i0 + 1;
+        r = r * 1664525u + 1013904223u;
+        float v1 = 0.0f;
+        if constexpr (i1 < LT::Q) v1 = float(d[i1]);
+        const uint32_t h2 = cvt_sr2<S>(v1, float(d[i0]), r ^ (r >> 16));
+        *reinterpret_cast<unsigned short *>(at(i0)) = (unsigned short)(h2 & 0xFFFFu);
+        if constexpr (i1 < LT::Q) *reinterpret_cast<unsigned short *>(at(i1)) = (unsigned short)(h2 >> 16);
+    });
+}
+
+// seed of a node's rounding stream: its index and its post-collision density
+// and velocity (so that it changes from step to step)
+template <typename T>
+__device__ __forceinline__ uint32_t sr_seed(uint32_t idx, T drho, T ux) {
+    return mix32(idx * 0x9E3779B9u ^ __float_as_uint(float(drho)) ^ (__float_as_uint(float(ux)) * 0x85EBCA6Bu));
 }
 
 // store a node's post-collision populations, coalesced across the warp
 template <class LT, typename S, typename T>
 __device__ __forceinline__ void store_node(S *__restrict__ fout, unsigned long long stride, uint32_t idx,
-                                           const T (&d)[LT::Q], bool sround) {
+                                           const T (&d)[LT::Q], bool sround, uint32_t seed) {
+    if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+        if (sround) {
+            store_sr_pairs<LT, S, T>(d, seed, [&](int i) { return fout + (unsigned long long)i * stride + idx; });
+            return;
+        }
+    }
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        S *p = fout + (unsigned long long)i * stride + idx;
-        if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
-            if (sround) {
-                // noise keyed by the value and the (node, population) slot
-                const uint32_t r = mix32(__float_as_uint(float(d[i])) ^ (idx * 0x9E3779B9u + (uint32_t)i * 0x85EBCA6Bu));
-                if constexpr (std::is_same<S, __half>::value) *p = f2h_sr(float(d[i]), r);
-                else *p = f2bf_sr(float(d[i]), r);
-                return;
-            }
-        }
-        st_dev<T>(p, d[i]);
+        st_dev<T>(fout + (unsigned long long)i * stride + idx, d[i]);
     });
 }
 
@@ -207,7 +232,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs<S> a) {
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
     collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
-    store_node<LT, S, T>(a.fout, a.g.stride, idx, d, a.g.sround != 0);
+    store_node<LT, S, T>(a.fout, a.g.stride, idx, d, a.g.sround != 0, sr_seed(idx, m.drho, ux));
 }
 
 // Division by a run-time constant d < 2^31 for numerators n < 2^31:
@@ -442,14 +467,7 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const _
     collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (g.sround) {
-            uint32_t r = mix32(idx * 0x9E3779B9u ^ __float_as_uint(float(m.drho)) ^
-                               (__float_as_uint(float(ux)) * 0x85EBCA6Bu));
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                r = r * 1664525u + 1013904223u;
-                if constexpr (std::is_same<S, __half>::value) a.dst[i][idx] = f2h_sr(float(d[i]), r >> 19);
-                else a.dst[i][idx] = f2bf_sr(float(d[i]), r >> 16);
-            });
+            store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
             return;
         }
     }

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256) les_step_kernel(const LesArgs<S> a) {
             if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
             const T om1 = T(1) - T(1) / (tau + taut);
             collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Fx, Fy, Fz);
-            store_node<LT, S, T>(a.fout, g.stride, idx, d, g.sround != 0);
+            store_node<LT, S, T>(a.fout, g.stride, idx, d, g.sround != 0, sr_seed(idx, m.drho, ux));
         }
         __syncthreads();
         const int t = sm;
