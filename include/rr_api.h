@@ -180,6 +180,59 @@ size_t rr_bytes_for(const rr_params *p);
 /* text of the last error on this thread ("" if none) */
 const char *rr_last_error(void);
 
+/* ---- Batches: many domains advanced together ------------------------------
+ * No counterpart in the reference, which runs one domain per process.  A
+ * batch steps every member solver in one persistent kernel launch per step
+ * (per storage type / lattice / forcing class; WALE members and grids with
+ * lx < 3 add their own launch), captured in CUDA graphs of 32 steps.  Each
+ * member's nodes get exactly the arithmetic of the member's own rr_step, so
+ * its results are the same alone and in a batch.
+ *
+ * While a solver is a member, its work runs on the batch's stream
+ * (rr_get_stream returns that stream); rr_macro, rr_get_f, rr_diag, rr_profile,
+ * rr_accumulate, rr_output and rr_save work as before, while rr_step,
+ * rr_init_state and rr_load return RR_ERR_STATE.  rr_destroy of a member
+ * removes it first. */
+typedef struct rr_batch rr_batch;
+
+rr_status rr_batch_create(int device, rr_batch **out);
+/* removes every member (waiting for the batch's work), then frees the batch */
+rr_status rr_batch_destroy(rr_batch *b);
+/* s must have a state (rr_init_state / rr_load), live on the batch's device
+ * and belong to no other batch */
+rr_status rr_batch_add(rr_batch *b, rr_solver *s);
+rr_status rr_batch_remove(rr_batch *b, rr_solver *s);
+int rr_batch_size(const rr_batch *b);
+/* advance every member by nsteps (enqueued on the batch's stream) */
+rr_status rr_batch_step(rr_batch *b, int nsteps);
+/* wait for the batch's work; RR_ERR_WATCHDOG if a member's watchdog fired
+ * (rr_last_error names the member, in order of addition) */
+rr_status rr_batch_sync(rr_batch *b);
+void *rr_batch_get_stream(const rr_batch *b);
+/* launch shape of the persistent kernel: threads per CTA (64, 128 or 256)
+ * and resident CTAs per SM (0: the kernel's occupancy limit) */
+rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm);
+rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm);
+
+/* ---- Autotuner ------------------------------------------------------------
+ * No counterpart in the reference (its launch shapes are the compile-time
+ * BLOCK_* of parameters.h).  Tries launch shapes on the solver's (or batch's)
+ * real steps, each for trial_steps steps timed with CUDA events, keeps the
+ * fastest and records it for the size class (lattice, storage, WALE, force,
+ * node count rounded to a power of two); solvers created later in that class
+ * start with it.  The shapes change no result, so the trial steps are
+ * ordinary steps: the state advances by (number of candidates) * trial_steps
+ * (reported in *steps_run).  Tile step: rows per work-item group; WALE step:
+ * the x-y tile and z chunk; batch: threads per CTA, CTAs per SM and the rows
+ * per group of each size class present.  Synchronises. */
+rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run);
+/* the solver's launch shapes: rows per work-item group of the tile step (a
+ * multiple of 32) and the WALE step's tile {tx, ty, z chunk}; les_tile may be
+ * NULL */
+rr_status rr_get_launch(const rr_solver *s, int *rows_group, int les_tile[3]);
+rr_status rr_set_launch(rr_solver *s, int rows_group, const int les_tile[3]);
+rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run);
+
 #ifdef __cplusplus
 }
 #endif

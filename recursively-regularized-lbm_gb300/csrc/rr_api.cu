@@ -18,6 +18,7 @@
 #include "rr_api.h"
 #include "rr_aux.h"
 #include "rr_dispatch.h"
+#include "rr_internal.h"
 #include "rr_kernels.cuh"
 
 namespace {
@@ -55,7 +56,6 @@ const rr::Ops &ops_for(int storage) {
 
 unsigned long long padded_stride(uint32_t n) { return ((unsigned long long)n + 63ull) & ~63ull; }
 
-bool has_force(const rr_params &p) { return p.force[0] != 0.0 || p.force[1] != 0.0 || p.force[2] != 0.0; }
 
 rr_status validate(const rr_params *p) {
     if (!p) return fail(RR_ERR_INVALID, "params is NULL");
@@ -92,31 +92,6 @@ rr_status validate(const rr_params *p) {
 }
 
 } // namespace
-
-struct rr_solver {
-    rr_params p;
-    const rr::Ops *ops = nullptr;
-    rr::Geom g{};
-    cudaStream_t stream = nullptr;
-    void *buf[2] = {nullptr, nullptr};
-    int cur = 0; // buffer holding the latest post-collision state
-    long long istep = 0;
-    bool ready = false;
-    bool stepped = false; // a step ran since the state was set: the previous buffer is valid
-    int *status = nullptr;   // device watchdog word
-    int *pos = nullptr;      // device: internal population -> API population
-    double *aux = nullptr;   // device FP64: rho, ux, uy, uz, taut (5 N)
-    double *stat = nullptr;  // device FP64: diag partials + outputs + profile + accumulators
-    long long acc_samples = 0;
-    size_t bytes = 0;
-    rr::LesTile tile{32, 8, 16};
-    rr::StepRange all{};      // every node, for grids with nx < 3 (general step)
-    uint32_t *all_list = nullptr;
-    uint32_t *edge_list = nullptr; // x-end nodes of rows on a y/z wall (tile step)
-    uint32_t nedges = 0;
-    int block = 256;
-    cudaGraphExec_t graph = nullptr;
-};
 
 namespace {
 
@@ -158,7 +133,7 @@ rr_status readout_macros(rr_solver *s, bool want_taut) {
     const size_t n = s->g.n;
     double *rho = s->aux, *ux = rho + n, *uy = ux + n, *uz = uy + n, *tt = uz + n;
     // the previous buffer holds the post-collision state the last step read
-    RR_CK(s->ops->readout(s->p.q, has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, nullptr, 0,
+    RR_CK(s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, nullptr, 0,
                           s->pos, rho, ux, uy, uz, s->stream));
     if (want_taut) RR_CK(rr::launch_wale(s->g, s->p.cw, ux, uy, uz, tt, s->stream));
     return RR_OK;
@@ -173,21 +148,9 @@ rr_status copy_out(rr_solver *s, double *dst, const double *src, size_t count, i
 }
 
 rr_status launch_steps(rr_solver *s, int n) {
-    const bool force = has_force(s->p);
-    const double om1 = 1.0 - 1.0 / s->p.tau;
     for (int k = 0; k < n; k++) {
-        const void *fin = s->buf[s->cur];
-        void *fout = s->buf[1 - s->cur];
-        if (s->p.use_les) {
-            RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force,
-                                   s->status, s->tile, s->stream));
-        } else if (s->p.lx >= 3) {
-            RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->edge_list,
-                               s->nedges, s->stream));
-        } else {
-            RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, om1, s->p.force, s->status, s->all,
-                               s->block, s->stream));
-        }
+        rr_status st = rr::launch_one(s, s->buf[s->cur], s->buf[1 - s->cur], s->stream);
+        if (st != RR_OK) return st;
         s->cur = 1 - s->cur;
     }
     return RR_OK;
@@ -232,6 +195,32 @@ rr_status ensure_dir(const char *dir) {
 }
 
 } // namespace
+
+namespace rr {
+
+bool has_force(const rr_params &p) { return p.force[0] != 0.0 || p.force[1] != 0.0 || p.force[2] != 0.0; }
+
+rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st) {
+    const bool force = rr::has_force(s->p);
+    if (s->p.use_les) {
+        RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status, s->tile,
+                               st));
+    } else if (s->p.lx >= 3) {
+        RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
+                           s->edge_list, s->nedges, s->rows_group, st));
+    } else {
+        RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status, s->all,
+                           s->block, st));
+    }
+    return RR_OK;
+}
+
+void drop_graph(rr_solver *s) {
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+}
+
+} // namespace rr
 
 // sets this thread's rr_last_error() text for entry points in other files
 rr_status rr_internal_error(rr_status st, const char *fmt, ...) {
@@ -310,6 +299,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     if (set_device(s) != RR_OK) return cleanup(RR_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess)
         return cleanup(fail(RR_ERR_CUDA, "stream creation failed"));
+    s->home = s->stream;
     const size_t bytes = (size_t)p->q * g.stride * s->ops->elem_bytes;
     for (int b = 0; b < 2; b++) {
         if (cudaMalloc(&s->buf[b], bytes) != cudaSuccess) {
@@ -384,6 +374,9 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     s->tile.tx = p->lx >= 32 ? 32 : 16;
     s->tile.ty = 256 / s->tile.tx;
     s->tile.zchunk = p->lz >= 64 ? 16 : (p->lz >= 16 ? 8 : p->lz);
+    // launch shapes the autotuner found for this size class, if any
+    rr::tuned_les_tile(*p, &s->tile);
+    rr::tuned_rows_group(*p, &s->rows_group);
     *out = s;
     return RR_OK;
 }
@@ -391,6 +384,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
 rr_status rr_destroy(rr_solver *s) {
     if (!s) return RR_OK;
     cudaSetDevice(s->p.device);
+    if (s->batch) rr::batch_detach(s);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     cudaFree(s->buf[0]);
@@ -400,7 +394,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->stat);
     cudaFree(s->all_list);
     cudaFree(s->edge_list);
-    if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->home) cudaStreamDestroy(s->home);
     cudaGetLastError();
     delete s;
     return RR_OK;
@@ -410,6 +404,7 @@ rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const 
                         const double *uy, const double *uz, int where) {
     if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
     if (!rho || !ux || !uy || !uz) return fail(RR_ERR_INVALID, "rho, ux, uy, uz are required");
+    if (s->batch) return fail(RR_ERR_STATE, "the solver is a member of a batch: remove it to set its state");
     if (set_device(s) != RR_OK) return RR_ERR_CUDA;
     const size_t n = s->g.n;
     const size_t nf = f ? (size_t)s->p.q * n : 0;
@@ -428,7 +423,7 @@ rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const 
     // the reference's first step computes tau_t from these macros (main.cu:375-379)
     if (e == cudaSuccess && s->p.use_les) e = rr::launch_wale(s->g, s->p.cw, d_ux, d_uy, d_uz, d_tt, s->stream);
     if (e == cudaSuccess)
-        e = s->ops->upload(s->p.q, has_force(s->p), s->buf[0], s->g, s->p.tau, s->p.force, d_f, n,
+        e = s->ops->upload(s->p.q, rr::has_force(s->p), s->buf[0], s->g, s->p.tau, s->p.force, d_f, n,
                            s->pos, d_rho, d_ux, d_uy, d_uz, s->p.use_les ? d_tt : nullptr, s->stream);
     cudaError_t e2 = cudaFreeAsync(tmp, s->stream);
     if (e != cudaSuccess) return fail(RR_ERR_CUDA, "state upload failed: %s", cudaGetErrorString(e));
@@ -449,6 +444,7 @@ rr_status rr_step(rr_solver *s, int nsteps) {
     if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
     if (!s->ready) return fail(RR_ERR_STATE, "rr_step before rr_init_state / rr_load");
     if (nsteps < 0) return fail(RR_ERR_INVALID, "nsteps = %d", nsteps);
+    if (s->batch) return fail(RR_ERR_STATE, "the solver is a member of a batch: step it with rr_batch_step");
     if (set_device(s) != RR_OK) return RR_ERR_CUDA;
     int left = nsteps;
     if (left >= 2 * GRAPH_STEPS) {
@@ -514,7 +510,7 @@ rr_status rr_get_f(rr_solver *s, double *f, int where) {
         RR_CK(cudaMallocAsync(&tmp, nf * sizeof(double), s->stream));
         dst = tmp;
     }
-    cudaError_t e = s->ops->readout(s->p.q, has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, dst,
+    cudaError_t e = s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, dst,
                                     n, s->pos, nullptr, nullptr, nullptr, nullptr, s->stream);
     if (e == cudaSuccess && tmp) e = cudaMemcpyAsync(f, tmp, nf * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
     if (tmp) cudaFreeAsync(tmp, s->stream);
@@ -640,6 +636,7 @@ rr_status rr_save(rr_solver *s, const char *dir) { return rr_output(s, RR_OUT_FL
 rr_status rr_load(rr_solver *s, const char *dir, long long istep) {
     // initialize() with CONTINUE_STEP > 0, initial.cu:189-265
     if (!s || !dir) return fail(RR_ERR_INVALID, "NULL argument");
+    if (s->batch) return fail(RR_ERR_STATE, "the solver is a member of a batch: remove it to set its state");
     const size_t n = s->g.n, nf = (size_t)s->p.q * n;
     std::vector<double> m(4 * n), f(nf);
     char name[64];

@@ -31,9 +31,22 @@ struct Ops {
                         cudaStream_t st);
     // one fused time step over the whole grid in one launch (needs nx >= 3);
     // edges: the x-end nodes of rows on a y/z wall face
+    // rows_group: rows per work-item group (a multiple of 32)
     cudaError_t (*tile)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const uint32_t *edges, uint32_t nedges,
-                        cudaStream_t st);
+                        int rows_group, cudaStream_t st);
+    // the tile step's descriptor of one domain (TileArgs, written to out when
+    // out != NULL) for a batch launch; returns its size, *nitems its warp items
+    size_t (*tile_desc)(int q, const void *fin, void *fout, const Geom &g, double om1, const double F[3],
+                        int *status, const uint32_t *edges, uint32_t nedges, int rows_group, void *out,
+                        uint32_t *nitems);
+    // one step of every domain of a batch: a persistent launch of `grid` CTAs
+    // of `block` threads over the domains' CTAs (cta_begin: [ndom + 1] prefix
+    // sums of ceil(32 nitems / block)); desc: device array of descriptors
+    cudaError_t (*batch)(int q, bool force, const void *desc, const uint32_t *cta_begin, uint32_t ndom,
+                         uint32_t total_ctas, int block, int grid, cudaStream_t st);
+    // resident CTAs per SM of the batch kernel (0 on error)
+    int (*batch_occupancy)(int q, bool force, int block);
     // fused time step with the WALE eddy viscosity
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,

@@ -1,0 +1,61 @@
+// rr_internal.h -- the solver object shared by the translation units of the
+// library (rr_api.cu: single domains; rr_batch.cu: batches and the
+// autotuner).  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "rr_api.h"
+#include "rr_dispatch.h"
+#include "rr_kernels.cuh"
+
+struct rr_solver {
+    rr_params p;
+    const rr::Ops *ops = nullptr;
+    rr::Geom g{};
+    cudaStream_t stream = nullptr; // where the solver's work goes (the batch's stream while a member)
+    cudaStream_t home = nullptr;   // the solver's own stream
+    rr_batch *batch = nullptr;     // batch the solver is a member of
+    void *buf[2] = {nullptr, nullptr};
+    int cur = 0; // buffer holding the latest post-collision state
+    long long istep = 0;
+    bool ready = false;
+    bool stepped = false; // a step ran since the state was set: the previous buffer is valid
+    int *status = nullptr;   // device watchdog word
+    int *pos = nullptr;      // device: internal population -> API population
+    double *aux = nullptr;   // device FP64: rho, ux, uy, uz, taut (5 N)
+    double *stat = nullptr;  // device FP64: diag partials + outputs + profile + accumulators
+    long long acc_samples = 0;
+    size_t bytes = 0;
+    rr::LesTile tile{32, 8, 16};
+    rr::StepRange all{};      // every node, for grids with nx < 3 (general step)
+    uint32_t *all_list = nullptr;
+    uint32_t *edge_list = nullptr; // x-end nodes of rows on a y/z wall (tile step)
+    uint32_t nedges = 0;
+    int block = 256;
+    int rows_group = 32; // tile step: rows per work-item group (autotuned)
+    cudaGraphExec_t graph = nullptr;
+};
+
+// sets this thread's rr_last_error() text and returns st
+rr_status rr_internal_error(rr_status st, const char *fmt, ...);
+
+namespace rr {
+
+bool has_force(const rr_params &p);
+// the step kind of a solver: the tile step (one launch, batchable) or not
+inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3; }
+// one step of s from fin to fout on stream st (state bookkeeping is the caller's)
+rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st);
+// drop the solver's captured step graph (launch shapes or buffers changed)
+void drop_graph(rr_solver *s);
+// tuned launch shapes of a size class, when the autotuner has seen it
+bool tuned_rows_group(const rr_params &p, int *rows_group);
+bool tuned_les_tile(const rr_params &p, LesTile *tile);
+// detach s from its batch (the batch's work on s is finished first)
+rr_status batch_detach(rr_solver *s);
+
+} // namespace rr

@@ -251,9 +251,10 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
 }
 
 // One-launch step with warp-granular work items.  The grid's warps walk
-// groups of ROWS_PER_ITEM_GROUP x-rows (row = z*ny + y).  A group holds, per
-// row, ceil((nx-2)/32) items of 32 consecutive nodes over x in [1, nx-2], and
-// then XFACE_ITEMS items with the x = 0 and the x = nx-1 nodes of its rows,
+// groups of rows_group x-rows (row = z*ny + y; rows_group a multiple of 32,
+// picked per size class by the autotuner).  A group holds, per row,
+// ceil((nx-2)/32) items of 32 consecutive nodes over x in [1, nx-2], and then
+// 2 rows_group / 32 items with the x = 0 and the x = nx-1 nodes of its rows,
 // 32 rows per item.  The x-face nodes are therefore processed in the same
 // window as their rows (the data they need sits in L2), they fill whole CTAs
 // of their own (a slow warp does not hold a CTA of fast ones resident), and
@@ -262,8 +263,6 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
 // periodic-edge rows and x-face items take the wrap-aware pull and, per node,
 // the closure of its wall face compiled for that face (edge and corner
 // nodes: the general face loop, out of line).
-constexpr int ROWS_PER_ITEM_GROUP = 32;
-constexpr int XFACE_ITEMS = 2 * ROWS_PER_ITEM_GROUP / 32; // x = 0 items, then x = nx-1 items
 
 template <int Q, typename S>
 struct TileArgs {
@@ -272,6 +271,7 @@ struct TileArgs {
     const S *fin;
     Geom g;
     uint32_t nitems, nrows, segs, group_items;
+    uint32_t rows_group, xf_half;    // rows per group; x-face items per face per group
     uint32_t nmain;                  // items of the row groups; the rest are edge items
     const uint32_t *edges;           // x-end nodes of rows on a y/z wall face
     uint32_t nedges;
@@ -354,11 +354,11 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 
 template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
 
-template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
+// one work item (one warp) of the tile step; A is TileArgs wherever it lives
+// (kernel parameters for one domain, shared memory for a batch)
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
     using T = typename CType<S>::T;
-    const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t lane = threadIdx.x & 31u;
     if (item >= a.nitems) return;
     const Geom &g = a.g;
     uint32_t row;
@@ -373,19 +373,19 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const _
         const uint32_t grp = fdiv(mitem, a.div_group);
         const uint32_t sub = mitem - grp * a.group_items;
         bool xface = false;
-        if (sub < ROWS_PER_ITEM_GROUP * a.segs) {
+        if (sub < a.rows_group * a.segs) {
             const uint32_t rl = fdiv(sub, a.div_segs);
-            row = grp * ROWS_PER_ITEM_GROUP + rl;
+            row = grp * a.rows_group + rl;
             x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
             fast = true;
             if (x > g.nx - 2) return;
         } else {
             // the x = 0 nodes of the group's rows, 32 per item, then the
             // x = nx-1 nodes: whole CTAs of these slower items
-            const uint32_t xi = sub - ROWS_PER_ITEM_GROUP * a.segs;
-            const uint32_t half = XFACE_ITEMS / 2;
-            row = grp * ROWS_PER_ITEM_GROUP + (xi % half) * 32u + lane;
-            x = xi < half ? 0 : g.nx - 1;
+            const uint32_t xi = sub - a.rows_group * a.segs;
+            const bool lo = xi < a.xf_half;
+            row = grp * a.rows_group + (lo ? xi : xi - a.xf_half) * 32u + lane;
+            x = lo ? 0 : g.nx - 1;
             fast = false;
             xface = true;
         }
@@ -475,6 +475,57 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const _
         constexpr int i = decltype(ic)::value;
         st_dev<T>(a.dst[i] + idx, d[i]);
     });
+}
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
+    tile_item<LT, S, FORCE>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+}
+
+// Many domains in one persistent launch.  The CTAs of every domain's tile
+// step (blockDim / 32 items each) are numbered consecutively, domain after
+// domain (cta_begin: prefix sums); the persistent grid strides over them.  A
+// CTA copies the descriptor of the domain it enters into shared memory and
+// runs the same work items as that domain's own tile launch, so every node
+// of a domain gets the arithmetic (and rounding stream) it gets alone.
+template <int Q, typename S>
+struct BatchArgs {
+    const TileArgs<Q, S> *desc; // per domain, for this step's buffer parity
+    const uint32_t *cta_begin;  // [ndom + 1]
+    uint32_t ndom, total_ctas;
+};
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256, tile_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs<LT::Q, S> b) {
+    using TA = TileArgs<LT::Q, S>;
+    static_assert(sizeof(TA) % 8 == 0, "descriptor copy is by 8-byte words");
+    __shared__ __align__(16) unsigned long long sdesc[sizeof(TA) / 8];
+    __shared__ uint32_t sdom;
+    const TA &a = *reinterpret_cast<const TA *>(sdesc);
+    const uint32_t wpc = blockDim.x >> 5; // items per CTA
+    uint32_t cur = 0xFFFFFFFFu;
+    for (uint32_t t = blockIdx.x; t < b.total_ctas; t += gridDim.x) {
+        if (threadIdx.x == 0) {
+            // last domain whose first CTA is <= t
+            uint32_t lo = 0, hi = b.ndom - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (__ldg(b.cta_begin + mid) <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            sdom = lo;
+        }
+        __syncthreads();
+        const uint32_t dom = sdom;
+        if (dom != cur) {
+            const unsigned long long *src = reinterpret_cast<const unsigned long long *>(b.desc + dom);
+            for (uint32_t w = threadIdx.x; w < sizeof(TA) / 8; w += blockDim.x) sdesc[w] = __ldg(src + w);
+            __syncthreads();
+            cur = dom;
+        }
+        tile_item<LT, S, FORCE>(a, (t - __ldg(b.cta_begin + dom)) * wpc + (threadIdx.x >> 5), threadIdx.x & 31u);
+        __syncthreads(); // sdom and sdesc are rewritten next iteration
+    }
 }
 
 // Readout: the reference's post-stream state after the last step, from the

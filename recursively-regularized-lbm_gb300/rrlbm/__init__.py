@@ -84,6 +84,20 @@ def lib():
             "rr_device_bytes": ([vp], ctypes.c_size_t),
             "rr_bytes_for": ([P], ctypes.c_size_t),
             "rr_last_error": ([], ctypes.c_char_p),
+            "rr_batch_create": ([ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
+            "rr_batch_destroy": ([vp], ctypes.c_int),
+            "rr_batch_add": ([vp, vp], ctypes.c_int),
+            "rr_batch_remove": ([vp, vp], ctypes.c_int),
+            "rr_batch_size": ([vp], ctypes.c_int),
+            "rr_batch_step": ([vp, ctypes.c_int], ctypes.c_int),
+            "rr_batch_sync": ([vp], ctypes.c_int),
+            "rr_batch_get_stream": ([vp], ctypes.c_void_p),
+            "rr_batch_set_launch": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+            "rr_batch_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+            "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+            "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_set_launch": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -231,6 +245,85 @@ class Solver:
 
     def load(self, directory, istep):
         _check(lib().rr_load(self._h, directory.encode(), int(istep)))
+
+    # -- launch shapes -------------------------------------------------------------
+    def tune(self, trial_steps=8):
+        """Autotune the launch shapes on real steps; returns the steps it ran."""
+        run = ctypes.c_longlong(0)
+        _check(lib().rr_tune(self._h, int(trial_steps), ctypes.byref(run)))
+        return run.value
+
+    def launch(self):
+        """(rows per work-item group, WALE tile (tx, ty, z chunk))."""
+        rg, t = ctypes.c_int(0), (ctypes.c_int * 3)()
+        _check(lib().rr_get_launch(self._h, ctypes.byref(rg), t))
+        return rg.value, tuple(t)
+
+    def set_launch(self, rows_group, les_tile=None):
+        t = None if les_tile is None else (ctypes.c_int * 3)(*les_tile)
+        _check(lib().rr_set_launch(self._h, int(rows_group), t))
+
+
+class Batch:
+    """Many solvers advanced together (rr_batch): one persistent launch per step."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().rr_batch_create(int(device), ctypes.byref(h)))
+        self._h = h
+        self._members = []
+
+    def close(self):
+        if self._h:
+            lib().rr_batch_destroy(self._h)
+            self._h = None
+            self._members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return lib().rr_batch_size(self._h)
+
+    def add(self, solver):
+        _check(lib().rr_batch_add(self._h, solver._h))
+        self._members.append(solver)
+
+    def remove(self, solver):
+        _check(lib().rr_batch_remove(self._h, solver._h))
+        self._members.remove(solver)
+
+    def step(self, n=1):
+        _check(lib().rr_batch_step(self._h, int(n)))
+
+    def sync(self):
+        _check(lib().rr_batch_sync(self._h))
+
+    @property
+    def stream(self):
+        return lib().rr_batch_get_stream(self._h) or 0
+
+    def set_launch(self, block, ctas_per_sm=0):
+        _check(lib().rr_batch_set_launch(self._h, int(block), int(ctas_per_sm)))
+
+    def launch(self):
+        b, c = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().rr_batch_get_launch(self._h, ctypes.byref(b), ctypes.byref(c)))
+        return b.value, c.value
+
+    def tune(self, trial_steps=8):
+        run = ctypes.c_longlong(0)
+        _check(lib().rr_batch_tune(self._h, int(trial_steps), ctypes.byref(run)))
+        return run.value
 
 
 from . import presets  # noqa: E402,F401

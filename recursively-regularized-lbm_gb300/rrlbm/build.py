@@ -15,9 +15,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-I", INCLUDE]
 SOURCES = ["rr_inst_f64.cu", "rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.cu",
-           "rr_aux.cu", "rr_api.cu", "rr_noalloc.cu"]
+           "rr_aux.cu", "rr_api.cu", "rr_batch.cu", "rr_noalloc.cu"]
 HEADERS = ["rr_lattice.cuh", "rr_node.cuh", "rr_node27.cuh", "rr_kernels.cuh", "rr_les.cuh", "rr_dispatch.h",
-           "rr_aux.h", "rr_inst.inc"]
+           "rr_aux.h", "rr_inst.inc", "rr_internal.h"]
 
 
 def _stale(target, deps):
