@@ -18,6 +18,17 @@ Line fields (one JSON line on rank 0):
              per lattice update.
   cpu_baseline  the oracle (C restatement of the reference step, OpenMP on
              all host threads) on a bounded sample of the same workload.
+  batch      the multi-domain form: 256 seeded Taylor-Green / cavity domains
+             (FP16 storage) advanced by one persistent launch per step inside
+             CUDA graphs, against the same domains stepped one at a time
+             (each domain's own rr_step, synchronised) and on concurrent
+             per-domain streams; aggregate MLUPS over a fixed step count.
+  serving    the served form: a seeded Poisson stream of Taylor-Green, cavity
+             and WALE channel solves (32^3-192^3, 1k-20k steps, FP16/FP32)
+             through the continuous-batching server under an 80 GB budget,
+             against a one-at-a-time server; solves/s, p50/p99 latency
+             (queueing and device parts) and each sampled solve's velocity
+             error against its FP64 rerun.
 --impl reference runs that CPU implementation alone as the reference arm.
 Multi-GPU (torchrun, N > 1): independent replicas, one domain per GPU.
 """
@@ -268,9 +279,8 @@ def run_gpu(args, rank, world, local_rank):
     if rank != 0:
         return
     pk, src = peaks()
-    # one launch over the wall-free box, one over the wall-node list (DNS);
-    # one tiled launch with the WALE eddy viscosity (LES)
-    launches_per_step = 1 if p.use_les else 2
+    # one launch per step: the tile step (DNS) or the WALE step (LES)
+    launches_per_step = 1
     bpl = 2 * q * BYTES_PER_POP[storage]
     achieved = n * bpl / (t_step * 1e-3) / 1e9
     traffic = ncu_traffic(args.workload)
@@ -294,7 +304,131 @@ def run_gpu(args, rank, world, local_rank):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
+    if world == 1 and args.batch_steps > 0:
+        line["batch"] = run_batch(args)
+        line["gpu_launches"] += line["batch"].pop("launches")
+    if world == 1 and args.serve_requests > 0:
+        line["serving"] = run_serve(args)
     print(json.dumps(line), flush=True)
+
+
+def run_batch(args):
+    """The multi-domain form: aggregate MLUPS of one batch against per-domain
+    launches, same domains, same step count."""
+    import torch
+    import rrlbm
+    from rrlbm import workloads
+
+    K = args.batch_steps
+    doms = workloads.ensemble(args.batch_domains, steps=K)
+    solvers = []
+    for d in doms:
+        s = rrlbm.Solver(workloads.params_of(d))
+        rho, ux, uy, uz = workloads.macros_on_device(d)
+        s.init_state(rho, ux, uy, uz)
+        s.sync()
+        solvers.append(s)
+    nodes = sum(d.nodes for d in doms)
+    out = {"domains": len(doms), "steps": K, "nodes": nodes, "storage": "f16",
+           "mix": "seeded: Taylor-Green cubes 32^3-128^3 (Ma 0.01-0.1, tau 0.52-0.8), "
+                  "cavities 32^3-96^3 (Re 100-1000), log-uniform sizes"}
+    # one at a time: each domain's own rr_step(K) (graphs of 32 steps), synchronised
+    for s in solvers:
+        s.step(2)
+        s.sync()
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.step(K)
+        s.sync()
+    t_seq = time.perf_counter() - t0
+    # per-domain launches on concurrent streams
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.step(K)
+    for s in solvers:
+        s.sync()
+    t_conc = time.perf_counter() - t0
+    # the batch: tuned launch shapes, then K steps timed on its stream
+    b = rrlbm.Batch()
+    for s in solvers:
+        b.add(s)
+    tune_steps = b.tune(trial_steps=8)
+    b.step(2 * 32)
+    b.sync()
+    st = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(st)
+    b.step(K)
+    e1.record(st)
+    b.sync()
+    t_batch = time.perf_counter() - t0
+    t_dev = e0.elapsed_time(e1) * 1e-3
+    block, cps = b.launch()
+    b.close()
+    for s in solvers:
+        s.close()
+    mlups = lambda t: nodes * K / t / 1e6
+    out.update({
+        "mlups": mlups(t_batch), "mlups_device": mlups(t_dev),
+        "mlups_one_at_a_time": mlups(t_seq), "mlups_concurrent_streams": mlups(t_conc),
+        "speedup_vs_one_at_a_time": t_seq / t_batch, "speedup_vs_concurrent_streams": t_conc / t_batch,
+        "tuned": {"block": block, "ctas_per_sm": cps, "tuning_steps": tune_steps},
+        "launches": K,  # one persistent launch per step (a single storage/lattice class)
+    })
+    return out
+
+
+def run_serve(args):
+    """The served form: continuous batching against one-at-a-time serving on
+    the same seeded request stream, and sampled errors against FP64 reruns."""
+    import numpy as np
+    from rrlbm import serve, workloads
+
+    reqs = workloads.request_stream(args.serve_requests, rate=200.0, seed=5)
+    budget = 80e9
+    # the solves whose FP64 rerun is affordable: the smallest by work, up to ~2e10 updates
+    order = sorted(reqs, key=lambda d: d.nodes * d.steps)
+    sample, work = set(), 0.0
+    for d in order:
+        if work + d.nodes * d.steps > 2e10 or len(sample) >= 8:
+            break
+        sample.add(d.rid)
+        work += d.nodes * d.steps
+    out = {"requests": len(reqs), "rate_per_s": 200.0, "budget_bytes": budget, "seed": 5,
+           "mix": "Poisson arrivals; Taylor-Green / cavity / WALE channel; n^3 with n in [32, 192] and "
+                  "steps in [1000, 20000] log-uniform; FP16 or FP32 storage, FP32 compute"}
+    for mode, slots in (("batched", None), ("one_at_a_time", 1)):
+        be = serve.GpuBackend()
+        # each solve's result: its domain means (rr_diag), read before it leaves
+        srv = serve.Server(be, budget, max_chunk=500, max_active=slots, on_result=lambda s: s.diag())
+        recs = srv.run(reqs)
+        be.close()
+        st = serve.summarize(recs)
+        st["chunks"] = srv.chunks
+        st["peak_resident"] = srv.peak_active
+        st["peak_bytes"] = srv.peak_bytes
+        out[mode] = st
+    # errors against FP64 reruns, sampled solves (served arithmetic = alone arithmetic,
+    # bit for bit, so the served result is the alone run)
+    errs = []
+    for d in reqs:
+        if d.rid not in sample:
+            continue
+        lo, hi = workloads.solve_alone(d), workloads.solve_alone(d, "f64")
+        a, b = lo.macro(), hi.macro()
+        lo.close()
+        hi.close()
+        u = workloads.velocity_scale(d)
+        e_max = max(float(np.abs(a[k] - b[k]).max()) for k in ("ux", "uy", "uz")) / u
+        num = sum(float(((a[k] - b[k]) ** 2).sum()) for k in ("ux", "uy", "uz"))
+        den = sum(float((b[k] ** 2).sum()) for k in ("ux", "uy", "uz"))
+        errs.append({"rid": d.rid, "kind": d.kind, "n": d.n, "steps": d.steps, "storage": d.storage,
+                     "max_err_rel_u": e_max, "l2_rel": (num / den) ** 0.5 if den > 0 else None})
+    out["fp64_rerun_errors"] = errs
+    out["speedup_solves_per_s"] = out["batched"]["solves_per_s"] / out["one_at_a_time"]["solves_per_s"]
+    return out
 
 
 def main():
@@ -307,6 +441,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device-timed steps only (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--batch-domains", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=1000, help="0: skip the multi-domain line")
+    ap.add_argument("--serve-requests", type=int, default=32, help="0: skip the serving line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
