@@ -67,6 +67,17 @@ def make(wl):
     return presets.taylor_green(L=100, nz=4, tau=0.6, Ma=0.01, storage=w["storage"])
 
 
+def describe(wl, p, storage):
+    kind = WORKLOADS[wl]["kind"]
+    if kind == "cavity":
+        return (f"lid-driven cavity {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Re=1000, lid 0.1 +x on y-hi, "
+                f"bounce-back + regularized closure on 6 faces, {storage} storage")
+    if kind == "channel":
+        return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 RR + WALE (C_w=0.5), Re_tau=180, walls y, periodic x/z, "
+                f"body force, {storage} storage")
+    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Ma=0.01, tau=0.6, periodic, {storage} storage"
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -102,7 +113,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -228,7 +239,7 @@ def run_gpu(args, rank, world, local_rank):
         # enqueues all K iterations, so host launch latency never lands
         # inside a timed window
         with torch.cuda.stream(stream):
-            torch.cuda._sleep(int(4e7 + 1e6 * K))
+            torch.cuda._sleep(int(4e7 + 5e4 * K))
         for k in range(K):
             with torch.cuda.stream(stream):
                 flush.fill_(float(k))  # evict the populations from L2
@@ -249,8 +260,11 @@ def run_gpu(args, rank, world, local_rank):
     if args.no_e2e:
         s.close()
         if rank == 0:
-            print(json.dumps({"value": value, "unit": "MLUPS", "ms_per_step": t_step,
-                              "workload": args.workload, "note": "profiling run, no e2e"}), flush=True)
+            line = {"value": value, "unit": "MLUPS", "ms_per_step": t_step, "workload": args.workload,
+                    "note": "profiling run, no e2e"}
+            if world == 1 and args.batch_steps > 0:
+                line["batch"] = run_batch(args)
+            print(json.dumps(line), flush=True)
         return
     # end to end through the C ABI with host buffers
     pin = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in ("rho", "ux", "uy", "uz")}
@@ -288,8 +302,7 @@ def run_gpu(args, rank, world, local_rank):
         "metric": "D3Q27 RR MLUPS (lattice updates per second)", "value": value, "unit": "MLUPS",
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[storage], "data": "synthetic",
-        "config": {"workload": f"lid-driven cavity {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Re=1000, lid 0.1 +x "
-                               f"on y-hi, bounce-back + regularized closure on 6 faces, {storage} storage",
+        "config": {"workload": describe(args.workload, p, storage),
                    "nodes": n, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed (256 MB write) before every timed step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -365,7 +378,7 @@ def run_batch(args):
     b.sync()
     t_batch = time.perf_counter() - t0
     t_dev = e0.elapsed_time(e1) * 1e-3
-    block, cps = b.launch()
+    block, cps, order = b.launch()
     b.close()
     for s in solvers:
         s.close()
@@ -374,7 +387,8 @@ def run_batch(args):
         "mlups": mlups(t_batch), "mlups_device": mlups(t_dev),
         "mlups_one_at_a_time": mlups(t_seq), "mlups_concurrent_streams": mlups(t_conc),
         "speedup_vs_one_at_a_time": t_seq / t_batch, "speedup_vs_concurrent_streams": t_conc / t_batch,
-        "tuned": {"block": block, "ctas_per_sm": cps, "tuning_steps": tune_steps},
+        "tuned": {"block": block, "ctas_per_sm": cps, "order": ["strided", "chunked"][order],
+                  "tuning_steps": tune_steps},
         "launches": K,  # one persistent launch per step (a single storage/lattice class)
     })
     return out
@@ -434,7 +448,7 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cavity128_f16", choices=sorted(WORKLOADS))

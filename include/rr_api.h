@@ -209,10 +209,12 @@ rr_status rr_batch_step(rr_batch *b, int nsteps);
  * (rr_last_error names the member, in order of addition) */
 rr_status rr_batch_sync(rr_batch *b);
 void *rr_batch_get_stream(const rr_batch *b);
-/* launch shape of the persistent kernel: threads per CTA (64, 128 or 256)
- * and resident CTAs per SM (0: the kernel's occupancy limit) */
-rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm);
-rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm);
+/* launch shape of the persistent kernel: threads per CTA (64, 128 or 256),
+ * resident CTAs per SM (0: the kernel's occupancy limit) and the order in
+ * which the persistent CTAs walk the members' CTAs */
+typedef enum { RR_BATCH_STRIDED = 0, RR_BATCH_CHUNKED = 1 } rr_batch_order;
+rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm, int order);
+rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, int *order);
 
 /* ---- Autotuner ------------------------------------------------------------
  * No counterpart in the reference (its launch shapes are the compile-time
@@ -223,8 +225,8 @@ rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm);
  * start with it.  The shapes change no result, so the trial steps are
  * ordinary steps: the state advances by (number of candidates) * trial_steps
  * (reported in *steps_run).  Tile step: rows per work-item group; WALE step:
- * the x-y tile and z chunk; batch: threads per CTA, CTAs per SM and the rows
- * per group of each size class present.  Synchronises. */
+ * the x-y tile and z chunk; batch: threads per CTA, CTAs per SM, walk order
+ * and the rows per group of each size class present.  Synchronises. */
 rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run);
 /* the solver's launch shapes: rows per work-item group of the tile step (a
  * multiple of 32) and the WALE step's tile {tx, ty, z chunk}; les_tile may be

@@ -45,6 +45,7 @@ struct Class {
     std::vector<rr_solver *> members;
     void *desc[2] = {nullptr, nullptr}; // device descriptor tables, per parity
     uint32_t *cta_begin = nullptr;      // device [members + 1]
+    uint32_t *cta_dom = nullptr;        // device [total_ctas]: member of each CTA
     uint32_t total_ctas = 0;
     int grid = 0;
 };
@@ -66,6 +67,7 @@ struct rr_batch {
     std::vector<rr_solver *> others; // members stepped by their own launch
     cudaGraphExec_t graph = nullptr;
     int block = 256, ctas_per_sm = 0;
+    int order = 0; // 0: strided walk over the CTAs, 1: contiguous chunks
     int sms = 0;
     int **status_ptrs = nullptr; // device: every member's watchdog word
     int *status_vals = nullptr;  // device
@@ -82,6 +84,7 @@ void drop_tables(rr_batch *b) {
         cudaFree(c.desc[0]);
         cudaFree(c.desc[1]);
         cudaFree(c.cta_begin);
+        cudaFree(c.cta_dom);
     }
     b->classes.clear();
     b->others.clear();
@@ -144,6 +147,15 @@ rr_status build_tables(rr_batch *b) {
             return rr_internal_error(RR_ERR_NOMEM, "cannot allocate the batch CTA table");
         }
         BK(cudaMemcpy(c.cta_begin, begin.data(), (nd + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        std::vector<uint32_t> dom(c.total_ctas);
+        for (size_t k = 0; k < nd; k++)
+            std::fill(dom.begin() + begin[k], dom.begin() + begin[k + 1], (uint32_t)k);
+        if (cudaMalloc(&c.cta_dom, std::max<size_t>(dom.size(), 1) * sizeof(uint32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            c.cta_dom = nullptr;
+            return rr_internal_error(RR_ERR_NOMEM, "cannot allocate the batch CTA map");
+        }
+        if (!dom.empty()) BK(cudaMemcpy(c.cta_dom, dom.data(), dom.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
         const int occ = c.ops->batch_occupancy(c.q, c.force, b->block);
         if (occ <= 0) return rr_internal_error(RR_ERR_CUDA, "batch kernel occupancy query failed");
         const int cps = b->ctas_per_sm > 0 ? std::min(b->ctas_per_sm, occ) : occ;
@@ -181,8 +193,8 @@ rr_status build_tables(rr_batch *b) {
 // one step of every member, reading the buffers of parity p
 rr_status launch_batch_step(rr_batch *b, int p) {
     for (Class &c : b->classes)
-        BK(c.ops->batch(c.q, c.force, c.desc[p], c.cta_begin, (uint32_t)c.members.size(), c.total_ctas, b->block,
-                        c.grid, b->stream));
+        BK(c.ops->batch(c.q, c.force, c.desc[p], c.cta_begin, c.cta_dom, (uint32_t)c.members.size(), c.total_ctas,
+                        b->block, c.grid, b->order, b->stream));
     for (rr_solver *s : b->others) {
         rr_status st = rr::launch_one(s, s->buf[p], s->buf[1 - p], b->stream);
         if (st != RR_OK) return st;
@@ -395,23 +407,27 @@ rr_status rr_batch_sync(rr_batch *b) {
     return RR_OK;
 }
 
-rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm) {
+rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm, int order) {
     if (!b) return rr_internal_error(RR_ERR_INVALID, "batch is NULL");
     if (block != 64 && block != 128 && block != 256)
         return rr_internal_error(RR_ERR_INVALID, "block = %d, must be 64, 128 or 256", block);
     if (ctas_per_sm < 0) return rr_internal_error(RR_ERR_INVALID, "ctas_per_sm = %d", ctas_per_sm);
-    if (block != b->block || ctas_per_sm != b->ctas_per_sm) {
+    if (order != RR_BATCH_STRIDED && order != RR_BATCH_CHUNKED)
+        return rr_internal_error(RR_ERR_INVALID, "order = %d unknown", order);
+    if (block != b->block || ctas_per_sm != b->ctas_per_sm || order != b->order) {
         b->block = block;
         b->ctas_per_sm = ctas_per_sm;
+        b->order = order;
         b->dirty = true;
     }
     return RR_OK;
 }
 
-rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm) {
+rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, int *order) {
     if (!b) return rr_internal_error(RR_ERR_INVALID, "batch is NULL");
     if (block) *block = b->block;
     if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm;
+    if (order) *order = b->order;
     return RR_OK;
 }
 
@@ -526,18 +542,19 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run) {
     for (rr_solver *s : b->members)
         if (rr::tile_step(s)) occ_max = std::max(occ_max, s->ops->batch_occupancy(s->p.q, rr::has_force(s->p), 128));
     struct Shape {
-        int block, cps;
+        int block, cps, order;
     };
     std::vector<Shape> shapes;
-    for (int block : {128, 256}) {
-        const int occ = std::max(1, block == 128 ? occ_max : occ_max / 2);
-        shapes.push_back(Shape{block, 0});
-        if (occ / 2 >= 1 && occ / 2 != occ) shapes.push_back(Shape{block, occ / 2});
-    }
+    for (int order : {RR_BATCH_STRIDED, RR_BATCH_CHUNKED})
+        for (int block : {128, 256}) {
+            const int occ = std::max(1, block == 128 ? occ_max : occ_max / 2);
+            shapes.push_back(Shape{block, 0, order});
+            if (occ / 2 >= 1 && occ / 2 != occ) shapes.push_back(Shape{block, occ / 2, order});
+        }
     float best = 1e30f;
-    Shape bs{b->block, b->ctas_per_sm};
+    Shape bs{b->block, b->ctas_per_sm, b->order};
     for (const Shape &sh : shapes) {
-        if ((st = rr_batch_set_launch(b, sh.block, sh.cps)) != RR_OK) return st;
+        if ((st = rr_batch_set_launch(b, sh.block, sh.cps, sh.order)) != RR_OK) return st;
         float ms = 0;
         if ((st = time_steps(b->stream, [&] { return step(trial); }, &ms)) != RR_OK) return st;
         if (ms < best) {
@@ -545,7 +562,7 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run) {
             bs = sh;
         }
     }
-    if ((st = rr_batch_set_launch(b, bs.block, bs.cps)) != RR_OK) return st;
+    if ((st = rr_batch_set_launch(b, bs.block, bs.cps, bs.order)) != RR_OK) return st;
     // 2. rows per work-item group, per size class of the tile-step members
     std::map<TuneKey, std::vector<rr_solver *>> by_class;
     for (rr_solver *s : b->members)

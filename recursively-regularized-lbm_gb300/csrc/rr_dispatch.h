@@ -42,9 +42,10 @@ struct Ops {
                         uint32_t *nitems);
     // one step of every domain of a batch: a persistent launch of `grid` CTAs
     // of `block` threads over the domains' CTAs (cta_begin: [ndom + 1] prefix
-    // sums of ceil(32 nitems / block)); desc: device array of descriptors
-    cudaError_t (*batch)(int q, bool force, const void *desc, const uint32_t *cta_begin, uint32_t ndom,
-                         uint32_t total_ctas, int block, int grid, cudaStream_t st);
+    // sums of ceil(32 nitems / block); cta_dom: domain of each CTA); desc:
+    // device array of descriptors; chunked: contiguous walk instead of strided
+    cudaError_t (*batch)(int q, bool force, const void *desc, const uint32_t *cta_begin, const uint32_t *cta_dom,
+                         uint32_t ndom, uint32_t total_ctas, int block, int grid, int chunked, cudaStream_t st);
     // resident CTAs per SM of the batch kernel (0 on error)
     int (*batch_occupancy)(int q, bool force, int block);
     // fused time step with the WALE eddy viscosity

@@ -484,15 +484,21 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const _
 
 // Many domains in one persistent launch.  The CTAs of every domain's tile
 // step (blockDim / 32 items each) are numbered consecutively, domain after
-// domain (cta_begin: prefix sums); the persistent grid strides over them.  A
-// CTA copies the descriptor of the domain it enters into shared memory and
-// runs the same work items as that domain's own tile launch, so every node
-// of a domain gets the arithmetic (and rounding stream) it gets alone.
+// domain (cta_begin: prefix sums; cta_dom: the domain of every CTA); the
+// persistent grid walks them either strided (CTA t of the grid takes t,
+// t + grid, ...) or in contiguous chunks.  A CTA copies the descriptor of the
+// domain it enters into shared memory and runs the same work items as that
+// domain's own tile launch, so every node of a domain gets the arithmetic
+// (and rounding stream) it gets alone.  The domain of the next CTA is read by
+// every thread (one broadcast load), so the threads agree without a barrier;
+// barriers are taken only around a descriptor change.
 template <int Q, typename S>
 struct BatchArgs {
     const TileArgs<Q, S> *desc; // per domain, for this step's buffer parity
     const uint32_t *cta_begin;  // [ndom + 1]
+    const uint32_t *cta_dom;    // [total_ctas]
     uint32_t ndom, total_ctas;
+    uint32_t chunk;             // 0: strided walk; else CTAs per persistent CTA
 };
 
 template <class LT, typename S, bool FORCE>
@@ -500,31 +506,30 @@ __global__ void __launch_bounds__(256, tile_min_blocks<S>()) batch_kernel(const 
     using TA = TileArgs<LT::Q, S>;
     static_assert(sizeof(TA) % 8 == 0, "descriptor copy is by 8-byte words");
     __shared__ __align__(16) unsigned long long sdesc[sizeof(TA) / 8];
-    __shared__ uint32_t sdom;
     const TA &a = *reinterpret_cast<const TA *>(sdesc);
     const uint32_t wpc = blockDim.x >> 5; // items per CTA
-    uint32_t cur = 0xFFFFFFFFu;
-    for (uint32_t t = blockIdx.x; t < b.total_ctas; t += gridDim.x) {
-        if (threadIdx.x == 0) {
-            // last domain whose first CTA is <= t
-            uint32_t lo = 0, hi = b.ndom - 1;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (__ldg(b.cta_begin + mid) <= t) lo = mid;
-                else hi = mid - 1;
-            }
-            sdom = lo;
-        }
-        __syncthreads();
-        const uint32_t dom = sdom;
+    uint32_t t, end, inc;
+    if (b.chunk) {
+        t = blockIdx.x * b.chunk;
+        end = min(t + b.chunk, b.total_ctas);
+        inc = 1;
+    } else {
+        t = blockIdx.x;
+        end = b.total_ctas;
+        inc = gridDim.x;
+    }
+    uint32_t cur = 0xFFFFFFFFu, first = 0;
+    for (; t < end; t += inc) {
+        const uint32_t dom = __ldg(b.cta_dom + t);
         if (dom != cur) {
+            if (cur != 0xFFFFFFFFu) __syncthreads(); // every warp is done with the old descriptor
             const unsigned long long *src = reinterpret_cast<const unsigned long long *>(b.desc + dom);
             for (uint32_t w = threadIdx.x; w < sizeof(TA) / 8; w += blockDim.x) sdesc[w] = __ldg(src + w);
             __syncthreads();
             cur = dom;
+            first = __ldg(b.cta_begin + dom);
         }
-        tile_item<LT, S, FORCE>(a, (t - __ldg(b.cta_begin + dom)) * wpc + (threadIdx.x >> 5), threadIdx.x & 31u);
-        __syncthreads(); // sdom and sdesc are rewritten next iteration
+        tile_item<LT, S, FORCE>(a, (t - first) * wpc + (threadIdx.x >> 5), threadIdx.x & 31u);
     }
 }
 

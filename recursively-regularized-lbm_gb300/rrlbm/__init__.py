@@ -92,8 +92,9 @@ def lib():
             "rr_batch_step": ([vp, ctypes.c_int], ctypes.c_int),
             "rr_batch_sync": ([vp], ctypes.c_int),
             "rr_batch_get_stream": ([vp], ctypes.c_void_p),
-            "rr_batch_set_launch": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
-            "rr_batch_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_batch_set_launch": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+            "rr_batch_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -312,13 +313,14 @@ class Batch:
     def stream(self):
         return lib().rr_batch_get_stream(self._h) or 0
 
-    def set_launch(self, block, ctas_per_sm=0):
-        _check(lib().rr_batch_set_launch(self._h, int(block), int(ctas_per_sm)))
+    def set_launch(self, block, ctas_per_sm=0, order=0):
+        """order: 0 strided walk, 1 contiguous chunks"""
+        _check(lib().rr_batch_set_launch(self._h, int(block), int(ctas_per_sm), int(order)))
 
     def launch(self):
-        b, c = ctypes.c_int(0), ctypes.c_int(0)
-        _check(lib().rr_batch_get_launch(self._h, ctypes.byref(b), ctypes.byref(c)))
-        return b.value, c.value
+        b, c, o = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().rr_batch_get_launch(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(o)))
+        return b.value, c.value, o.value
 
     def tune(self, trial_steps=8):
         run = ctypes.c_longlong(0)

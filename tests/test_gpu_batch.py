@@ -99,8 +99,8 @@ def test_batch_watchdog_names_member():
     sb.close()
 
 
-@pytest.mark.parametrize("block,cps", [(64, 0), (128, 1), (256, 2)])
-def test_launch_shapes_change_nothing(block, cps):
+@pytest.mark.parametrize("block,cps,order", [(64, 0, 0), (128, 1, 1), (256, 2, 0), (256, 0, 1)])
+def test_launch_shapes_change_nothing(block, cps, order):
     doms = _domains()[:4]
     ref = []
     for p, st in doms:
@@ -111,8 +111,8 @@ def test_launch_shapes_change_nothing(block, cps):
     for s in solvers:
         s.set_launch(64 if block == 64 else 32)
     with rrlbm.Batch() as b:
-        b.set_launch(block, cps)
-        assert b.launch() == (block, cps)
+        b.set_launch(block, cps, order)
+        assert b.launch() == (block, cps, order)
         for s in solvers:
             b.add(s)
         b.step(9)

@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _small_stream():
-    reqs = workloads.request_stream(7, rate=400.0, seed=11, sizes=(10, 22), steps=(20, 150))
+    reqs = workloads.request_stream(7, rate=400.0, seed=12, sizes=(10, 22), steps=(20, 150))
     kinds = [d.kind for d in reqs]
     assert len(set(kinds)) == 3, kinds
     return reqs
