@@ -224,15 +224,19 @@ rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, i
  * node count rounded to a power of two); solvers created later in that class
  * start with it.  The shapes change no result, so the trial steps are
  * ordinary steps: the state advances by (number of candidates) * trial_steps
- * (reported in *steps_run).  Tile step: rows per work-item group; WALE step:
- * the x-y tile and z chunk; batch: threads per CTA, CTAs per SM, walk order
+ * (reported in *steps_run).  Tile step and two-pass WALE step: rows per
+ * work-item group; fused WALE step: the x-y tile and z chunk (the WALE method
+ * itself is not tuned: the two methods round differently); batch: threads per CTA, CTAs per SM, walk order
  * and the rows per group of each size class present.  Synchronises. */
 rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run);
 /* the solver's launch shapes: rows per work-item group of the tile step (a
- * multiple of 32) and the WALE step's tile {tx, ty, z chunk}; les_tile may be
- * NULL */
-rr_status rr_get_launch(const rr_solver *s, int *rows_group, int les_tile[3]);
-rr_status rr_set_launch(rr_solver *s, int rows_group, const int les_tile[3]);
+ * multiple of 32); the WALE step's method (RR_LES_FUSED: one launch of
+ * z-marching tiles {tx, ty, z chunk} with a shared-memory velocity ring;
+ * RR_LES_TWO_PASS: two tile-step launches through a velocity field, lx >= 3);
+ * les_method and les_tile may be NULL */
+typedef enum { RR_LES_FUSED = 0, RR_LES_TWO_PASS = 1 } rr_les_method;
+rr_status rr_get_launch(const rr_solver *s, int *rows_group, int *les_method, int les_tile[3]);
+rr_status rr_set_launch(rr_solver *s, int rows_group, const int *les_method, const int les_tile[3]);
 rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run);
 
 #ifdef __cplusplus

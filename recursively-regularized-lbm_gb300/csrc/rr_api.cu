@@ -56,6 +56,13 @@ const rr::Ops &ops_for(int storage) {
 
 unsigned long long padded_stride(uint32_t n) { return ((unsigned long long)n + 63ull) & ~63ull; }
 
+// velocity field of the two-pass WALE step (compute type: FP64 for FP64 storage)
+size_t les_ubuf_bytes(const rr_params &p) {
+    if (!p.use_les || p.lx < 3) return 0;
+    const uint32_t n = (uint32_t)p.lx * p.ly * p.lz;
+    return 3 * padded_stride(n) * (p.storage == RR_STORE_F64 ? sizeof(double) : sizeof(float));
+}
+
 
 rr_status validate(const rr_params *p) {
     if (!p) return fail(RR_ERR_INVALID, "params is NULL");
@@ -203,8 +210,12 @@ bool has_force(const rr_params &p) { return p.force[0] != 0.0 || p.force[1] != 0
 rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st) {
     const bool force = rr::has_force(s->p);
     if (s->p.use_les) {
-        RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status, s->tile,
-                               st));
+        if (s->les_method == RR_LES_TWO_PASS && s->ubuf)
+            RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
+                               s->edge_list, s->nedges, s->rows_group, s->ubuf, st));
+        else
+            RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
+                                   s->tile, st));
     } else if (s->p.lx >= 3) {
         RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
                            s->edge_list, s->nedges, s->rows_group, st));
@@ -263,7 +274,11 @@ size_t rr_bytes_for(const rr_params *p) {
     if (!p || validate(p) != RR_OK) return 0;
     const uint32_t n = (uint32_t)p->lx * p->ly * p->lz;
     const size_t elem = p->storage == RR_STORE_F64 ? 8 : p->storage == RR_STORE_F32 ? 4 : 2;
-    return 2 * (size_t)p->q * padded_stride(n) * elem + 256 + stat_doubles(*p) * sizeof(double);
+    size_t b = 2 * (size_t)p->q * padded_stride(n) * elem + 256 + stat_doubles(*p) * sizeof(double);
+    b += les_ubuf_bytes(*p);
+    // edge-node list of the tile step (x-ends of the rows on a y/z wall face)
+    if (p->lx >= 3) b += 2 * sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
+    return b;
 }
 
 rr_status rr_create(const rr_params *p, rr_solver **out) {
@@ -370,6 +385,17 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         s->bytes += lb;
     }
     g.sround = (p->rounding == RR_ROUND_STOCHASTIC) ? 1 : 0;
+    if (const size_t ub = les_ubuf_bytes(*p)) {
+        if (cudaMalloc(&s->ubuf, ub) != cudaSuccess) {
+            cudaGetLastError();
+            s->ubuf = nullptr;
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of WALE velocity field", ub));
+        }
+        s->bytes += ub;
+        s->les_method = RR_LES_TWO_PASS;
+    } else {
+        s->les_method = RR_LES_FUSED;
+    }
     // LES tile by size class: full 32-wide rows when x allows, else 16
     s->tile.tx = p->lx >= 32 ? 32 : 16;
     s->tile.ty = 256 / s->tile.tx;
@@ -394,6 +420,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->stat);
     cudaFree(s->all_list);
     cudaFree(s->edge_list);
+    cudaFree(s->ubuf);
     if (s->home) cudaStreamDestroy(s->home);
     cudaGetLastError();
     delete s;

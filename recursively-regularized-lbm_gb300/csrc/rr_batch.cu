@@ -431,9 +431,10 @@ rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, i
     return RR_OK;
 }
 
-rr_status rr_get_launch(const rr_solver *s, int *rows_group, int les_tile[3]) {
+rr_status rr_get_launch(const rr_solver *s, int *rows_group, int *les_method, int les_tile[3]) {
     if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
     if (rows_group) *rows_group = s->rows_group;
+    if (les_method) *les_method = s->les_method;
     if (les_tile) {
         les_tile[0] = s->tile.tx;
         les_tile[1] = s->tile.ty;
@@ -442,8 +443,16 @@ rr_status rr_get_launch(const rr_solver *s, int *rows_group, int les_tile[3]) {
     return RR_OK;
 }
 
-rr_status rr_set_launch(rr_solver *s, int rows_group, const int les_tile[3]) {
+rr_status rr_set_launch(rr_solver *s, int rows_group, const int *les_method, const int les_tile[3]) {
     if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
+    int method = s->les_method;
+    if (les_method) {
+        method = *les_method;
+        if (method != RR_LES_FUSED && method != RR_LES_TWO_PASS)
+            return rr_internal_error(RR_ERR_INVALID, "les_method = %d unknown", method);
+        if (method == RR_LES_TWO_PASS && !s->ubuf)
+            return rr_internal_error(RR_ERR_INVALID, "the two-pass WALE step needs use_les and lx >= 3");
+    }
     if (rows_group < 32 || rows_group % 32 != 0 || rows_group > 4096)
         return rr_internal_error(RR_ERR_INVALID, "rows_group = %d, must be a multiple of 32 in [32, 4096]", rows_group);
     rr::LesTile t = s->tile;
@@ -455,9 +464,11 @@ rr_status rr_set_launch(rr_solver *s, int rows_group, const int les_tile[3]) {
             return rr_internal_error(RR_ERR_INVALID, "WALE tile %dx%d (z chunk %d): need tx*ty <= 256, a multiple of 32",
                                      t.tx, t.ty, t.zchunk);
     }
-    if (rows_group != s->rows_group || t.tx != s->tile.tx || t.ty != s->tile.ty || t.zchunk != s->tile.zchunk) {
+    if (rows_group != s->rows_group || t.tx != s->tile.tx || t.ty != s->tile.ty || t.zchunk != s->tile.zchunk ||
+        method != s->les_method) {
         s->rows_group = rows_group;
         s->tile = t;
+        s->les_method = method;
         rr::drop_graph(s);
         if (s->batch) s->batch->dirty = true;
     }
@@ -478,7 +489,10 @@ rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run) {
     rr_status st = step(1); // first launches (module load) outside the timings
     if (st != RR_OK) return st;
     const int trial = std::min(trial_steps, 63); // plain launches, no graph capture per candidate
-    if (s->p.use_les) {
+    if (s->p.use_les && s->les_method == RR_LES_FUSED) {
+        // the fused WALE step: x-y tile and z chunk.  (The two WALE methods
+        // round differently in FP32, so the method is the caller's choice and
+        // the tuner keeps it.)
         std::vector<rr::LesTile> cands;
         const int zcs[3] = {8, 16, 32};
         const int shapes[4][2] = {{32, 8}, {64, 4}, {32, 4}, {16, 16}};
@@ -499,7 +513,8 @@ rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run) {
         s->tile = bt;
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_les_tile[tune_key(s->p)] = bt;
-    } else if (rr::tile_step(s)) {
+    } else if (rr::tile_step(s) || s->les_method == RR_LES_TWO_PASS) {
+        // the tile step, or the two tile passes of the WALE step: rows per group
         const int cands[3] = {32, 64, 128};
         float best = 1e30f;
         int br = s->rows_group;

@@ -52,6 +52,11 @@ struct Ops {
     cudaError_t (*step_les)(int q, bool force, const void *fin, void *fout, const Geom &g,
                             double tau, double cw, const double F[3], int *status,
                             const LesTile &tile, cudaStream_t st);
+    // the same step in two tile launches (needs nx >= 3): velocities into ubuf
+    // (3 arrays of g.stride in the compute type), then tau_t + collision
+    cudaError_t (*les2)(int q, bool force, const void *fin, void *fout, const Geom &g, double tau, double cw,
+                        const double F[3], int *status, const uint32_t *edges, uint32_t nedges, int rows_group,
+                        void *ubuf, cudaStream_t st);
     // post-stream populations / macroscopic fields from the post-collision buffer
     cudaError_t (*readout)(int q, bool force, const void *fin, const Geom &g, const double F[3],
                            double *fo, unsigned long long fo_stride, const int *pos, double *rho,

@@ -30,7 +30,9 @@ struct rr_solver {
     double *stat = nullptr;  // device FP64: diag partials + outputs + profile + accumulators
     long long acc_samples = 0;
     size_t bytes = 0;
-    rr::LesTile tile{32, 8, 16};
+    rr::LesTile tile{32, 8, 16};    // fused WALE step: x-y tile and z chunk
+    int les_method = RR_LES_FUSED; // WALE step: fused z-marching tiles or two tile passes
+    void *ubuf = nullptr;          // two-pass WALE step: velocity field (3 arrays of g.stride)
     rr::StepRange all{};      // every node, for grids with nx < 3 (general step)
     uint32_t *all_list = nullptr;
     uint32_t *edge_list = nullptr; // x-end nodes of rows on a y/z wall (tile step)

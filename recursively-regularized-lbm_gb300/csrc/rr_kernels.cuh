@@ -281,6 +281,8 @@ struct TileArgs {
     double om1;
     double F[3];
     int *status;
+    typename CType<S>::T *u; // WALE passes: velocity field, 3 arrays of g.stride
+    double tau, cw;          // WALE collide pass: molecular tau, C_w
 };
 
 // populations entering the domain through face F (0..5 = x-lo .. z-hi)
@@ -354,9 +356,69 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 
 template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
 
+template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
+template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
+template <> __device__ __forceinline__ double rr_sqrt(double v) { return sqrt(v); }
+
+// WALE tau_t of LES.cu:79-97 from the velocity gradient g[a][b] = du_a/dx_b.
+// x^1.5, x^2.5 and x^1.25 are formed from square roots; S:S = Sd:Sd = 0 gives 0
+// where the reference gives 0/0.
+template <typename T>
+__device__ __forceinline__ T wale_tau_t(const T (&gr)[3][3], T cw) {
+    const T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
+    const T dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
+    const T dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
+    T sijsq = (dudy + dvdx) * (dudy + dvdx) + (dudz + dwdx) * (dudz + dwdx) + (dvdz + dwdy) * (dvdz + dwdy);
+    sijsq = T(0.5) * sijsq + dudx * dudx + dvdy * dvdy + dwdz * dwdz;
+    const T third = T(1) / T(3);
+    T s11d = (T(2) * dudx * dudx - dvdy * dvdy - dwdz * dwdz + dudy * dvdx + dudz * dwdx - T(2) * dvdz * dwdy) * third;
+    T s12d = T(0.5) * (dudx * (dudy + dvdx) + dudy * dvdy + dvdx * dvdy + dvdz * dwdx + dudz * dwdy);
+    T s13d = T(0.5) * (dudx * (dudz + dwdx) + dudy * dvdz + dvdx * dwdy + dudz * dwdz + dwdx * dwdz);
+    T s22d = (T(2) * dvdy * dvdy - dudx * dudx - dwdz * dwdz + dudy * dvdx + dvdz * dwdy - T(2) * dudz * dwdx) * third;
+    T s23d = T(0.5) * (dvdy * (dvdz + dwdy) + dudz * dvdx + dudy * dwdx + dvdz * dwdz + dwdy * dwdz);
+    T s33d = (T(2) * dwdz * dwdz - dudx * dudx - dvdy * dvdy + dudz * dwdx + dvdz * dwdy - T(2) * dudy * dvdx) * third;
+    T sd = s11d * s11d + s22d * s22d + s33d * s33d + T(2) * (s12d * s12d + s13d * s13d + s23d * s23d);
+    const T rs = rr_sqrt(sijsq), rd = rr_sqrt(sd);
+    const T den = sijsq * sijsq * rs + sd * rr_sqrt(rd); // S:S^2.5 + Sd:Sd^1.25
+    return den > T(0) ? T(3) * cw * cw * (sd * rd) / den : T(0);
+}
+
+// tau_t of node (x, y, z) from the velocity field u (3 arrays of g.stride):
+// central differences with periodic wrap, the reference's one-sided
+// differences (3 u0 + u1) / 3 and (-3 u_{N-1} - u_{N-2}) / 3 on wall faces
+// (LES.cu:20-78)
+template <typename T>
+__device__ __forceinline__ T les_taut(const T *__restrict__ u, const Geom &g, int x, int y, int z, uint32_t idx,
+                                      T cw) {
+    const uint32_t nx = (uint32_t)g.nx, nxy = (uint32_t)g.nx * (uint32_t)g.ny;
+    const uint32_t ixm = x == 0 ? idx + nx - 1u : idx - 1u;
+    const uint32_t ixp = x == g.nx - 1 ? idx - (nx - 1u) : idx + 1u;
+    const uint32_t iym = y == 0 ? idx + (uint32_t)(g.ny - 1) * nx : idx - nx;
+    const uint32_t iyp = y == g.ny - 1 ? idx - (uint32_t)(g.ny - 1) * nx : idx + nx;
+    const uint32_t izm = z == 0 ? idx + (uint32_t)(g.nz - 1) * nxy : idx - nxy;
+    const uint32_t izp = z == g.nz - 1 ? idx - (uint32_t)(g.nz - 1) * nxy : idx + nxy;
+    const bool xlo = x == 0 && g.face[0] != FACE_PERIODIC, xhi = x == g.nx - 1 && g.face[1] != FACE_PERIODIC;
+    const bool ylo = y == 0 && g.face[2] != FACE_PERIODIC, yhi = y == g.ny - 1 && g.face[3] != FACE_PERIODIC;
+    const bool zlo = z == 0 && g.face[4] != FACE_PERIODIC, zhi = z == g.nz - 1 && g.face[5] != FACE_PERIODIC;
+    T gr[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const T *q = u + (unsigned long long)k * g.stride;
+        const T uc = q[idx];
+        const T xm = q[ixm], xp = q[ixp], ym = q[iym], yp = q[iyp], zm = q[izm], zp = q[izp];
+        gr[k][0] = xlo ? (T(3) * uc + xp) / T(3) : (xhi ? (T(-3) * uc - xm) / T(3) : T(0.5) * (xp - xm));
+        gr[k][1] = ylo ? (T(3) * uc + yp) / T(3) : (yhi ? (T(-3) * uc - ym) / T(3) : T(0.5) * (yp - ym));
+        gr[k][2] = zlo ? (T(3) * uc + zp) / T(3) : (zhi ? (T(-3) * uc - zm) / T(3) : T(0.5) * (zp - zm));
+    }
+    return wale_tau_t(gr, cw);
+}
+
 // one work item (one warp) of the tile step; A is TileArgs wherever it lives
-// (kernel parameters for one domain, shared memory for a batch)
-template <class LT, typename S, bool FORCE, class A>
+// (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
+// DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
+// applies the walls and writes the velocity field; MODE 2 streams again,
+// takes tau_t from the 7-point stencil of that field and collides.
+template <class LT, typename S, bool FORCE, int MODE = 0, class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
     using T = typename CType<S>::T;
     if (item >= a.nitems) return;
@@ -463,8 +525,16 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if constexpr (MODE == 1) {
+        a.u[idx] = ux;
+        a.u[g.stride + idx] = uy;
+        a.u[2ull * g.stride + idx] = uz;
+        return;
+    }
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
-    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+    T om1 = T(a.om1);
+    if constexpr (MODE == 2) om1 = T(1) - T(1) / (T(a.tau) + les_taut<T>(a.u, g, x, y, z, idx, T(a.cw)));
+    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Fx, Fy, Fz);
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (g.sround) {
             store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
@@ -477,9 +547,9 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     });
 }
 
-template <class LT, typename S, bool FORCE>
+template <class LT, typename S, bool FORCE, int MODE = 0>
 __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    tile_item<LT, S, FORCE>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+    tile_item<LT, S, FORCE, MODE>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
 
 // Many domains in one persistent launch.  The CTAs of every domain's tile

@@ -21,33 +21,6 @@
 
 namespace rr {
 
-template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
-template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
-template <> __device__ __forceinline__ double rr_sqrt(double v) { return sqrt(v); }
-
-// WALE tau_t of LES.cu:79-97 from the velocity gradient g[a][b] = du_a/dx_b.
-// x^1.5, x^2.5 and x^1.25 are formed from square roots; S:S = Sd:Sd = 0 gives 0
-// where the reference gives 0/0.
-template <typename T>
-__device__ __forceinline__ T wale_tau_t(const T (&gr)[3][3], T cw) {
-    const T dudx = gr[0][0], dudy = gr[0][1], dudz = gr[0][2];
-    const T dvdx = gr[1][0], dvdy = gr[1][1], dvdz = gr[1][2];
-    const T dwdx = gr[2][0], dwdy = gr[2][1], dwdz = gr[2][2];
-    T sijsq = (dudy + dvdx) * (dudy + dvdx) + (dudz + dwdx) * (dudz + dwdx) + (dvdz + dwdy) * (dvdz + dwdy);
-    sijsq = T(0.5) * sijsq + dudx * dudx + dvdy * dvdy + dwdz * dwdz;
-    const T third = T(1) / T(3);
-    T s11d = (T(2) * dudx * dudx - dvdy * dvdy - dwdz * dwdz + dudy * dvdx + dudz * dwdx - T(2) * dvdz * dwdy) * third;
-    T s12d = T(0.5) * (dudx * (dudy + dvdx) + dudy * dvdy + dvdx * dvdy + dvdz * dwdx + dudz * dwdy);
-    T s13d = T(0.5) * (dudx * (dudz + dwdx) + dudy * dvdz + dvdx * dwdy + dudz * dwdz + dwdx * dwdz);
-    T s22d = (T(2) * dvdy * dvdy - dudx * dudx - dwdz * dwdz + dudy * dvdx + dvdz * dwdy - T(2) * dudz * dwdx) * third;
-    T s23d = T(0.5) * (dvdy * (dvdz + dwdy) + dudz * dvdx + dudy * dwdx + dvdz * dwdz + dwdy * dwdz);
-    T s33d = (T(2) * dwdz * dwdz - dudx * dudx - dvdy * dvdy + dudz * dwdx + dvdz * dwdy - T(2) * dudy * dvdx) * third;
-    T sd = s11d * s11d + s22d * s22d + s33d * s33d + T(2) * (s12d * s12d + s13d * s13d + s23d * s23d);
-    const T rs = rr_sqrt(sijsq), rd = rr_sqrt(sd);
-    const T den = sijsq * sijsq * rs + sd * rr_sqrt(rd); // S:S^2.5 + Sd:Sd^1.25
-    return den > T(0) ? T(3) * cw * cw * (sd * rd) / den : T(0);
-}
-
 template <typename S>
 struct LesArgs {
     const S *__restrict__ fin;

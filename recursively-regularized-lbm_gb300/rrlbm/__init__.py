@@ -97,8 +97,10 @@ def lib():
                                      ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
-            "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
-            "rr_set_launch": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                               ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_set_launch": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+                              ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -255,14 +257,15 @@ class Solver:
         return run.value
 
     def launch(self):
-        """(rows per work-item group, WALE tile (tx, ty, z chunk))."""
-        rg, t = ctypes.c_int(0), (ctypes.c_int * 3)()
-        _check(lib().rr_get_launch(self._h, ctypes.byref(rg), t))
-        return rg.value, tuple(t)
+        """(rows per work-item group, WALE method (0 fused, 1 two-pass), WALE tile (tx, ty, z chunk))."""
+        rg, m, t = ctypes.c_int(0), ctypes.c_int(0), (ctypes.c_int * 3)()
+        _check(lib().rr_get_launch(self._h, ctypes.byref(rg), ctypes.byref(m), t))
+        return rg.value, m.value, tuple(t)
 
-    def set_launch(self, rows_group, les_tile=None):
+    def set_launch(self, rows_group, les_method=None, les_tile=None):
+        m = None if les_method is None else ctypes.byref(ctypes.c_int(int(les_method)))
         t = None if les_tile is None else (ctypes.c_int * 3)(*les_tile)
-        _check(lib().rr_set_launch(self._h, int(rows_group), t))
+        _check(lib().rr_set_launch(self._h, int(rows_group), m, t))
 
 
 class Batch:

@@ -148,8 +148,8 @@ def test_autotuners_keep_results():
             s.step(3)
             r.step(run + 3)
             assert np.array_equal(s.get_f(), r.get_f())
-            rg, tile = s.launch()
-            assert rg % 32 == 0 and tile[0] * tile[1] <= 256
+            rg, method, tile = s.launch()
+            assert rg % 32 == 0 and method in (0, 1) and tile[0] * tile[1] <= 256
             # the size class remembers the shape for later solvers
             with rrlbm.Solver(p) as t:
                 assert t.launch() == s.launch()

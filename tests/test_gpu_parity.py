@@ -18,10 +18,13 @@ TOL_U = 1e-12   # relative to the velocity scale
 TOL_RHO = 1e-13 # absolute on rho and on f
 
 
-def _run_pair(p, st, steps, les=None):
+def _run_pair(p, st, steps, les=None, les_method=None):
     o = oracle_for(p, les)
     load_state(o, st)
     with rrlbm.Solver(p) as s:
+        if les_method is not None:
+            s.set_launch(s.launch()[0], les_method=les_method)
+            assert s.launch()[1] == les_method
         s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
         done = 0
         out = []
@@ -80,24 +83,32 @@ def test_channel_dns_reference_start():
     _check(_run_pair(p, st, [1, 20, 100]), st["ustar"] * 20)
 
 
-def test_channel_les_reference_start():
+LES_METHODS = [0, 1]  # RR_LES_FUSED (z-marching tiles), RR_LES_TWO_PASS (two tile launches)
+
+
+@pytest.mark.parametrize("method", LES_METHODS)
+def test_channel_les_reference_start(method):
     p, st = presets.channel(nx=16, ny=12, nz=8, les=True, variant="reference")
-    _check(_run_pair(p, st, [1, 20, 60]), st["ustar"] * 20)
+    _check(_run_pair(p, st, [1, 20, 60], les_method=method), st["ustar"] * 20)
 
 
-def test_channel_les_noise_start():
+@pytest.mark.parametrize("method", LES_METHODS)
+def test_channel_les_noise_start(method):
     # a start with all three velocity components and large gradients
     p, st = presets.channel(nx=40, ny=20, nz=12, les=True, variant="config", amp=0.3)
-    _check(_run_pair(p, st, [1, 15]), st["uc"])
+    _check(_run_pair(p, st, [1, 15], les_method=method), st["uc"])
 
 
-def test_les_partial_tiles_and_forcing_axes():
-    # grid not a multiple of the tile, force on all axes, walls on x
+@pytest.mark.parametrize("method", LES_METHODS)
+def test_les_partial_tiles_and_forcing_axes(method):
+    # grid not a multiple of the tile, force on all axes, walls on x and z
     p, st = presets.channel(nx=37, ny=11, nz=5, les=True, variant="config", amp=0.3)
     p.face[0] = p.face[1] = rrlbm.FACE_WALL
+    if method == 1:
+        p.face[4] = p.face[5] = rrlbm.FACE_WALL_BB
     p.force[1] = 1e-6
     p.force[2] = -2e-6
-    _check(_run_pair(p, st, [1, 12]), st["uc"])
+    _check(_run_pair(p, st, [1, 12], les_method=method), st["uc"])
 
 
 @pytest.mark.parametrize("dims", [(34, 7, 5), (2, 9, 6), (3, 3, 3), (67, 5, 4)])
