@@ -366,19 +366,28 @@ def run_batch(args):
     for s in solvers:
         b.add(s)
     tune_steps = b.tune(trial_steps=8)
-    b.step(2 * 32)
-    b.sync()
     st = torch.cuda.ExternalStream(b.stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e0.record(st)
-    b.step(K)
-    e1.record(st)
-    b.sync()
-    t_batch = time.perf_counter() - t0
-    t_dev = e0.elapsed_time(e1) * 1e-3
+
+    def timed():
+        b.step(2 * 32)
+        b.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(st)
+        b.step(K)
+        e1.record(st)
+        b.sync()
+        return time.perf_counter() - t0, e0.elapsed_time(e1) * 1e-3
+
+    mode, chains = b.mode()
     block, cps, order = b.launch()
+    t_batch, t_dev = timed()
+    # the other mode, for the record
+    b.set_mode(1 - mode, chains)
+    t_other, _ = timed()
+    b.set_mode(mode, chains)
+    grouping = b.grouping
     b.close()
     for s in solvers:
         s.close()
@@ -387,9 +396,13 @@ def run_batch(args):
         "mlups": mlups(t_batch), "mlups_device": mlups(t_dev),
         "mlups_one_at_a_time": mlups(t_seq), "mlups_concurrent_streams": mlups(t_conc),
         "speedup_vs_one_at_a_time": t_seq / t_batch, "speedup_vs_concurrent_streams": t_conc / t_batch,
-        "tuned": {"block": block, "ctas_per_sm": cps, "order": ["strided", "chunked"][order],
-                  "tuning_steps": tune_steps},
-        "launches": K,  # one persistent launch per step (a single storage/lattice class)
+        "mode": ["persistent kernel", "fan-out of member launches"][mode],
+        f"mlups_{['fanout', 'persistent'][mode]}": mlups(t_other),
+        "tuned": {"mode": mode, "chains": chains, "block": block, "ctas_per_sm": cps,
+                  "order": ["strided", "chunked"][order], "grouping_bytes": grouping, "tuning_steps": tune_steps},
+        # persistent: one launch per step and class (a single storage/lattice class here);
+        # fan-out: every member's own launch per step
+        "launches": K if mode == 0 else K * len(doms),
     })
     return out
 

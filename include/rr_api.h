@@ -215,6 +215,21 @@ void *rr_batch_get_stream(const rr_batch *b);
 typedef enum { RR_BATCH_STRIDED = 0, RR_BATCH_CHUNKED = 1 } rr_batch_order;
 rr_status rr_batch_set_launch(rr_batch *b, int block, int ctas_per_sm, int order);
 rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, int *order);
+/* how a step of the batch is launched: RR_BATCH_PERSISTENT, one persistent
+ * batch kernel per class (above); RR_BATCH_FANOUT, each member's own step
+ * launches, the members spread over `chains` parallel branches of the graph
+ * (largest first to the least loaded branch), a branch running its members'
+ * steps member after member.  Same results either way. */
+typedef enum { RR_BATCH_PERSISTENT = 0, RR_BATCH_FANOUT = 1 } rr_batch_mode;
+rr_status rr_batch_set_mode(rr_batch *b, int mode, int chains);
+rr_status rr_batch_get_mode(const rr_batch *b, int *mode, int *chains);
+/* L2 grouping: members whose population buffers fit are packed (in order of
+ * addition, per class) into groups of at most group_bytes, and each group
+ * runs its steps of an rr_batch_step back to back, so its data stays in L2
+ * across steps; larger members share one launch per step.  0 turns grouping
+ * off (the default). */
+rr_status rr_batch_set_grouping(rr_batch *b, size_t group_bytes);
+size_t rr_batch_get_grouping(const rr_batch *b);
 
 /* ---- Autotuner ------------------------------------------------------------
  * No counterpart in the reference (its launch shapes are the compile-time
@@ -226,8 +241,10 @@ rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, i
  * ordinary steps: the state advances by (number of candidates) * trial_steps
  * (reported in *steps_run).  Tile step and two-pass WALE step: rows per
  * work-item group; fused WALE step: the x-y tile and z chunk (the WALE method
- * itself is not tuned: the two methods round differently); batch: threads per CTA, CTAs per SM, walk order
- * and the rows per group of each size class present.  Synchronises. */
+ * itself is not tuned: the two methods round differently); batch: the mode
+ * (fan-out chains 4, 8, 16 or the persistent kernel), threads per CTA, CTAs per
+ * SM, walk order, L2 grouping and the rows per group of each size class
+ * present.  Synchronises. */
 rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run);
 /* the solver's launch shapes: rows per work-item group of the tile step (a
  * multiple of 32); the WALE step's method (RR_LES_FUSED: one launch of

@@ -28,6 +28,7 @@
 namespace {
 
 constexpr int BATCH_GRAPH_STEPS = 32; // steps per captured graph (even: ends on the same parity)
+constexpr int MAX_CHAINS = 32;        // fan-out mode: most parallel chains
 
 #define BK(call)                                                                                  \
     do {                                                                                          \
@@ -37,7 +38,8 @@ constexpr int BATCH_GRAPH_STEPS = 32; // steps per captured graph (even: ends on
                                      cudaGetErrorString(e_), __FILE__, __LINE__);                 \
     } while (0)
 
-// members that share one persistent launch
+// members that share one persistent launch: one (storage, lattice, forcing)
+// class, and either members small enough to stay in L2 together or the rest
 struct Class {
     const rr::Ops *ops = nullptr;
     int q = 27;
@@ -48,6 +50,7 @@ struct Class {
     uint32_t *cta_dom = nullptr;        // device [total_ctas]: member of each CTA
     uint32_t total_ctas = 0;
     int grid = 0;
+    size_t bytes = 0; // population buffers of the members
 };
 
 __global__ void gather_status(int *const *ptrs, int n, int *out) {
@@ -68,6 +71,14 @@ struct rr_batch {
     cudaGraphExec_t graph = nullptr;
     int block = 256, ctas_per_sm = 0;
     int order = 0; // 0: strided walk over the CTAs, 1: contiguous chunks
+    size_t group_bytes = 0; // members whose buffers fit are grouped up to this size and run
+                            // their steps back to back (L2 reuse); 0: no grouping
+    int mode = RR_BATCH_PERSISTENT;
+    int chains = 8;                                 // fan-out mode: parallel chains
+    std::vector<cudaStream_t> side;                 // one stream per chain
+    std::vector<cudaEvent_t> side_done;             // one event per chain
+    cudaEvent_t fork = nullptr;
+    std::vector<std::vector<rr_solver *>> chain;    // members of each chain
     int sms = 0;
     int **status_ptrs = nullptr; // device: every member's watchdog word
     int *status_vals = nullptr;  // device
@@ -94,25 +105,34 @@ rr_status build_tables(rr_batch *b) {
     if (!b->dirty) return RR_OK;
     BK(cudaStreamSynchronize(b->stream)); // the old tables may still be read
     drop_tables(b);
+    // per class: members larger than group_bytes share one launch group; the
+    // others are packed, in order of addition, into groups of at most
+    // group_bytes of population buffers
+    std::vector<Class> big;
     for (rr_solver *s : b->members) {
         if (!rr::tile_step(s)) {
             b->others.push_back(s);
             continue;
         }
         const bool force = rr::has_force(s->p);
-        auto it = std::find_if(b->classes.begin(), b->classes.end(), [&](const Class &c) {
-            return c.ops == s->ops && c.q == s->p.q && c.force == force;
+        const size_t fb = 2 * (size_t)s->p.q * s->g.stride * s->ops->elem_bytes;
+        const bool small = b->group_bytes > 0 && fb <= b->group_bytes;
+        std::vector<Class> &pool = small ? b->classes : big;
+        auto it = std::find_if(pool.begin(), pool.end(), [&](const Class &c) {
+            return c.ops == s->ops && c.q == s->p.q && c.force == force && (!small || c.bytes + fb <= b->group_bytes);
         });
-        if (it == b->classes.end()) {
+        if (it == pool.end()) {
             Class c;
             c.ops = s->ops;
             c.q = s->p.q;
             c.force = force;
-            b->classes.push_back(c);
-            it = b->classes.end() - 1;
+            pool.push_back(c);
+            it = pool.end() - 1;
         }
         it->members.push_back(s);
+        it->bytes += fb;
     }
+    b->classes.insert(b->classes.end(), big.begin(), big.end());
     for (Class &c : b->classes) {
         const size_t nd = c.members.size();
         const rr_solver *s0 = c.members[0];
@@ -162,6 +182,20 @@ rr_status build_tables(rr_batch *b) {
         c.grid = (int)std::min<unsigned long long>(c.total_ctas, (unsigned long long)cps * b->sms);
         if (c.grid < 1) c.grid = 1;
     }
+    // fan-out chains: members by decreasing size, each to the least loaded chain
+    b->chain.assign(b->chains, {});
+    {
+        std::vector<rr_solver *> order(b->members);
+        std::stable_sort(order.begin(), order.end(), [](const rr_solver *x, const rr_solver *y) {
+            return (size_t)x->g.n * x->ops->elem_bytes > (size_t)y->g.n * y->ops->elem_bytes;
+        });
+        std::vector<double> load(b->chains, 0.0);
+        for (rr_solver *s : order) {
+            const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            b->chain[c].push_back(s);
+            load[c] += (double)s->g.n * (s->p.use_les ? 2.0 : 1.0) * (double)s->ops->elem_bytes;
+        }
+    }
     // watchdog gather table
     const int n = (int)b->members.size();
     if (n > b->status_cap) {
@@ -190,15 +224,39 @@ rr_status build_tables(rr_batch *b) {
     return RR_OK;
 }
 
-// one step of every member, reading the buffers of parity p
-rr_status launch_batch_step(rr_batch *b, int p) {
-    for (Class &c : b->classes)
-        BK(c.ops->batch(c.q, c.force, c.desc[p], c.cta_begin, c.cta_dom, (uint32_t)c.members.size(), c.total_ctas,
-                        b->block, c.grid, b->order, b->stream));
-    for (rr_solver *s : b->others) {
-        rr_status st = rr::launch_one(s, s->buf[p], s->buf[1 - p], b->stream);
-        if (st != RR_OK) return st;
+// n steps of every member from buffer parity p, group after group (a group's
+// steps run back to back, so a group that fits in L2 stays there)
+rr_status launch_batch_steps(rr_batch *b, int p, int n) {
+    if (b->mode == RR_BATCH_FANOUT) {
+        // every chain forks from the batch stream, runs its members' n steps
+        // member after member, and joins back
+        BK(cudaEventRecord(b->fork, b->stream));
+        for (int c = 0; c < b->chains; c++) {
+            if (b->chain[c].empty()) continue;
+            BK(cudaStreamWaitEvent(b->side[c], b->fork, 0));
+            for (rr_solver *s : b->chain[c])
+                for (int k = 0; k < n; k++) {
+                    const int q = p ^ (k & 1);
+                    rr_status st = rr::launch_one(s, s->buf[q], s->buf[1 - q], b->side[c]);
+                    if (st != RR_OK) return st;
+                }
+            BK(cudaEventRecord(b->side_done[c], b->side[c]));
+            BK(cudaStreamWaitEvent(b->stream, b->side_done[c], 0));
+        }
+        return RR_OK;
     }
+    for (Class &c : b->classes)
+        for (int k = 0; k < n; k++) {
+            const int q = p ^ (k & 1);
+            BK(c.ops->batch(c.q, c.force, c.desc[q], c.cta_begin, c.cta_dom, (uint32_t)c.members.size(),
+                            c.total_ctas, b->block, c.grid, b->order, b->stream));
+        }
+    for (rr_solver *s : b->others)
+        for (int k = 0; k < n; k++) {
+            const int q = p ^ (k & 1);
+            rr_status st = rr::launch_one(s, s->buf[q], s->buf[1 - q], b->stream);
+            if (st != RR_OK) return st;
+        }
     return RR_OK;
 }
 
@@ -207,7 +265,7 @@ rr_status build_graph(rr_batch *b) {
     cudaGraph_t graph;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     rr_status st = RR_OK;
-    for (int k = 0; k < BATCH_GRAPH_STEPS && st == RR_OK; k++) st = launch_batch_step(b, k & 1);
+    st = launch_batch_steps(b, 0, BATCH_GRAPH_STEPS);
     cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
     if (st != RR_OK) {
         if (e == cudaSuccess) cudaGraphDestroy(graph);
@@ -289,11 +347,25 @@ rr_status rr_batch_create(int device, rr_batch **out) {
     BK(cudaSetDevice(device));
     rr_batch *b = new rr_batch;
     b->device = device;
+    int l2 = 0;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device) != cudaSuccess) {
         cudaGetLastError();
         if (b->stream) cudaStreamDestroy(b->stream);
         delete b;
+        return rr_internal_error(RR_ERR_CUDA, "batch stream creation failed");
+    }
+    b->group_bytes = 0;
+    b->side.assign(MAX_CHAINS, nullptr);
+    b->side_done.assign(MAX_CHAINS, nullptr);
+    bool ok = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int c = 0; c < MAX_CHAINS && ok; c++)
+        ok = cudaStreamCreateWithFlags(&b->side[c], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&b->side_done[c], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        rr_batch_destroy(b);
         return rr_internal_error(RR_ERR_CUDA, "batch stream creation failed");
     }
     *out = b;
@@ -309,6 +381,11 @@ rr_status rr_batch_destroy(rr_batch *b) {
     cudaFree(b->status_ptrs);
     cudaFree(b->status_vals);
     cudaFreeHost(b->status_host);
+    for (cudaStream_t st : b->side)
+        if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : b->side_done)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
     cudaStreamDestroy(b->stream);
     cudaGetLastError();
     delete b;
@@ -362,7 +439,7 @@ rr_status rr_batch_step(rr_batch *b, int nsteps) {
     int left = nsteps;
     if (left >= 2 * BATCH_GRAPH_STEPS) {
         if (b->parity != 0) {
-            if ((st = launch_batch_step(b, 1)) != RR_OK) return st;
+            if ((st = launch_batch_steps(b, 1, 1)) != RR_OK) return st;
             b->parity = 0;
             left--;
         }
@@ -372,10 +449,9 @@ rr_status rr_batch_step(rr_batch *b, int nsteps) {
             left -= BATCH_GRAPH_STEPS;
         }
     }
-    while (left > 0) {
-        if ((st = launch_batch_step(b, b->parity)) != RR_OK) return st;
-        b->parity ^= 1;
-        left--;
+    if (left > 0) {
+        if ((st = launch_batch_steps(b, b->parity, left)) != RR_OK) return st;
+        b->parity ^= left & 1;
     }
     for (rr_solver *s : b->members) {
         s->cur = b->parity;
@@ -430,6 +506,38 @@ rr_status rr_batch_get_launch(const rr_batch *b, int *block, int *ctas_per_sm, i
     if (order) *order = b->order;
     return RR_OK;
 }
+
+rr_status rr_batch_set_mode(rr_batch *b, int mode, int chains) {
+    if (!b) return rr_internal_error(RR_ERR_INVALID, "batch is NULL");
+    if (mode != RR_BATCH_PERSISTENT && mode != RR_BATCH_FANOUT)
+        return rr_internal_error(RR_ERR_INVALID, "mode = %d unknown", mode);
+    if (chains < 1 || chains > MAX_CHAINS)
+        return rr_internal_error(RR_ERR_INVALID, "chains = %d, must be 1 to %d", chains, MAX_CHAINS);
+    if (mode != b->mode || chains != b->chains) {
+        b->mode = mode;
+        b->chains = chains;
+        b->dirty = true;
+    }
+    return RR_OK;
+}
+
+rr_status rr_batch_get_mode(const rr_batch *b, int *mode, int *chains) {
+    if (!b) return rr_internal_error(RR_ERR_INVALID, "batch is NULL");
+    if (mode) *mode = b->mode;
+    if (chains) *chains = b->chains;
+    return RR_OK;
+}
+
+rr_status rr_batch_set_grouping(rr_batch *b, size_t group_bytes) {
+    if (!b) return rr_internal_error(RR_ERR_INVALID, "batch is NULL");
+    if (group_bytes != b->group_bytes) {
+        b->group_bytes = group_bytes;
+        b->dirty = true;
+    }
+    return RR_OK;
+}
+
+size_t rr_batch_get_grouping(const rr_batch *b) { return b ? b->group_bytes : 0; }
 
 rr_status rr_get_launch(const rr_solver *s, int *rows_group, int *les_method, int les_tile[3]) {
     if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
@@ -552,6 +660,19 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run) {
     };
     rr_status st = step(1);
     if (st != RR_OK) return st;
+    // 0. fan-out chains (the members' own launches on parallel graph branches)
+    float best_fan = 1e30f;
+    int best_chains = b->chains;
+    for (int ch : {4, 8, 16}) {
+        if ((st = rr_batch_set_mode(b, RR_BATCH_FANOUT, ch)) != RR_OK) return st;
+        float ms = 0;
+        if ((st = time_steps(b->stream, [&] { return step(trial); }, &ms)) != RR_OK) return st;
+        if (ms < best_fan) {
+            best_fan = ms;
+            best_chains = ch;
+        }
+    }
+    if ((st = rr_batch_set_mode(b, RR_BATCH_PERSISTENT, best_chains)) != RR_OK) return st;
     // 1. threads per CTA and CTAs per SM of the persistent launch
     int occ_max = 0;
     for (rr_solver *s : b->members)
@@ -578,7 +699,28 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run) {
         }
     }
     if ((st = rr_batch_set_launch(b, bs.block, bs.cps, bs.order)) != RR_OK) return st;
-    // 2. rows per work-item group, per size class of the tile-step members
+    // 2. L2 grouping of the small members: none, a quarter, half of L2
+    {
+        int l2 = 0;
+        BK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, b->device));
+        const size_t cands[3] = {0, (size_t)l2 / 4, (size_t)l2 / 2};
+        size_t bg = b->group_bytes;
+        float bt = 1e30f;
+        for (size_t gb : cands) {
+            if ((st = rr_batch_set_grouping(b, gb)) != RR_OK) return st;
+            float ms = 0;
+            if ((st = time_steps(b->stream, [&] { return step(trial); }, &ms)) != RR_OK) return st;
+            if (ms < bt) {
+                bt = ms;
+                bg = gb;
+            }
+        }
+        if ((st = rr_batch_set_grouping(b, bg)) != RR_OK) return st;
+        if (best_fan < std::min(best, bt)) {
+            if ((st = rr_batch_set_mode(b, RR_BATCH_FANOUT, best_chains)) != RR_OK) return st;
+        }
+    }
+    // 3. rows per work-item group, per size class of the tile-step members
     std::map<TuneKey, std::vector<rr_solver *>> by_class;
     for (rr_solver *s : b->members)
         if (rr::tile_step(s)) by_class[tune_key(s->p)].push_back(s);

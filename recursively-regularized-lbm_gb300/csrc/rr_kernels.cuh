@@ -355,6 +355,9 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 }
 
 template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
+// the batch kernel holds its loop state and the shared descriptor on top of
+// the tile step: one CTA less per SM keeps its spills down
+template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : 4; }
 
 template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
 template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
@@ -572,7 +575,7 @@ struct BatchArgs {
 };
 
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256, tile_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs<LT::Q, S> b) {
+__global__ void __launch_bounds__(256, batch_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs<LT::Q, S> b) {
     using TA = TileArgs<LT::Q, S>;
     static_assert(sizeof(TA) % 8 == 0, "descriptor copy is by 8-byte words");
     __shared__ __align__(16) unsigned long long sdesc[sizeof(TA) / 8];

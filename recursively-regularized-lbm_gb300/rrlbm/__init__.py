@@ -95,6 +95,10 @@ def lib():
             "rr_batch_set_launch": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
             "rr_batch_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                      ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_batch_set_grouping": ([vp, ctypes.c_size_t], ctypes.c_int),
+            "rr_batch_set_mode": ([vp, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+            "rr_batch_get_mode": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+            "rr_batch_get_grouping": ([vp], ctypes.c_size_t),
             "rr_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
@@ -329,6 +333,24 @@ class Batch:
         run = ctypes.c_longlong(0)
         _check(lib().rr_batch_tune(self._h, int(trial_steps), ctypes.byref(run)))
         return run.value
+
+    def set_mode(self, mode, chains=8):
+        """mode: 0 persistent kernel, 1 fan-out of the members' own launches over parallel chains"""
+        _check(lib().rr_batch_set_mode(self._h, int(mode), int(chains)))
+
+    def mode(self):
+        m, c = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().rr_batch_get_mode(self._h, ctypes.byref(m), ctypes.byref(c)))
+        return m.value, c.value
+
+    @property
+    def grouping(self):
+        """bytes up to which small members are grouped for L2 reuse (0: off)"""
+        return lib().rr_batch_get_grouping(self._h)
+
+    @grouping.setter
+    def grouping(self, nbytes):
+        _check(lib().rr_batch_set_grouping(self._h, int(nbytes)))
 
 
 from . import presets  # noqa: E402,F401

@@ -50,12 +50,16 @@ class GpuBackend:
 
     READOUT_BYTES_PER_NODE = 40  # FP64 rho, u, tau_t scratch a readout allocates
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, mode=1, chains=16):
+        """mode 1 (default): the members' own launches fanned over `chains`
+        parallel graph branches; mode 0: one persistent batch kernel per step
+        (rr_batch_set_mode)"""
         import rrlbm
 
         self._rr = rrlbm
         self.device = device
         self.batch = rrlbm.Batch(device)
+        self.batch.set_mode(mode, chains)
         self.members = []  # handles in order of addition (the batch's member order)
 
     def bytes_for(self, d):

@@ -34,7 +34,8 @@ def _solver(p, st):
     return s
 
 
-def test_alone_vs_mix_bit_identical():
+@pytest.mark.parametrize("mode", [0, 1])
+def test_alone_vs_mix_bit_identical(mode):
     doms = _domains()
     late = presets.cavity(n=16, Re=300, storage="f16")  # joins on the other buffer parity
     steps_early, steps = 3, 70  # 70 >= 64: the graph path plus single launches
@@ -48,6 +49,7 @@ def test_alone_vs_mix_bit_identical():
         alone_late = s.get_f()
     solvers = [_solver(p, st) for p, st in doms]
     with rrlbm.Batch() as b:
+        b.set_mode(mode, 4)
         for s in solvers:
             b.add(s)
         b.step(steps_early)
@@ -99,8 +101,10 @@ def test_batch_watchdog_names_member():
     sb.close()
 
 
-@pytest.mark.parametrize("block,cps,order", [(64, 0, 0), (128, 1, 1), (256, 2, 0), (256, 0, 1)])
-def test_launch_shapes_change_nothing(block, cps, order):
+@pytest.mark.parametrize("block,cps,order,group,mode", [(64, 0, 0, 0, 0), (128, 1, 1, 1 << 20, 0),
+                                                        (256, 2, 0, 8 << 20, 0), (256, 0, 1, 64 << 20, 0),
+                                                        (256, 0, 0, 0, 1)])
+def test_launch_shapes_change_nothing(block, cps, order, group, mode):
     doms = _domains()[:4]
     ref = []
     for p, st in doms:
@@ -112,10 +116,13 @@ def test_launch_shapes_change_nothing(block, cps, order):
         s.set_launch(64 if block == 64 else 32)
     with rrlbm.Batch() as b:
         b.set_launch(block, cps, order)
-        assert b.launch() == (block, cps, order)
+        b.grouping = group
+        b.set_mode(mode, 3)
+        assert b.launch() == (block, cps, order) and b.grouping == group and b.mode() == (mode, 3)
         for s in solvers:
             b.add(s)
-        b.step(9)
+        b.step(2)
+        b.step(7)  # odd parity at the start of a grouped run
         for k, s in enumerate(solvers):
             assert np.array_equal(s.get_f(), ref[k])
     for s in solvers:
