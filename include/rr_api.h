@@ -240,7 +240,8 @@ size_t rr_batch_get_grouping(const rr_batch *b);
  * start with it.  The shapes change no result, so the trial steps are
  * ordinary steps: the state advances by (number of candidates) * trial_steps
  * (reported in *steps_run).  Tile step and two-pass WALE step: rows per
- * work-item group; fused WALE step: the x-y tile and z chunk (the WALE method
+ * work-item group; DNS: tile or staged step, the staged block rows and
+ * stages; fused WALE step: the x-y tile and z chunk (the WALE method
  * itself is not tuned: the two methods round differently); batch: the mode
  * (fan-out chains 4, 8, 16 or the persistent kernel), threads per CTA, CTAs per
  * SM, walk order, L2 grouping and the rows per group of each size class
@@ -255,6 +256,14 @@ typedef enum { RR_LES_FUSED = 0, RR_LES_TWO_PASS = 1 } rr_les_method;
 rr_status rr_get_launch(const rr_solver *s, int *rows_group, int *les_method, int les_tile[3]);
 rr_status rr_set_launch(rr_solver *s, int rows_group, const int *les_method, const int les_tile[3]);
 rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run);
+/* the DNS step's method: RR_DNS_TILE, one launch of warp work items (any
+ * grid with lx >= 3); RR_DNS_STAGED, rows on a y/z face in one launch and the
+ * interior rows in blocks of `rows` rows through a `stages`-deep pipeline of
+ * bulk copies into shared memory (DNS, lx, ly, lz >= 3, lx times the element
+ * size a multiple of 16 bytes).  Same results bit for bit. */
+typedef enum { RR_DNS_TILE = 0, RR_DNS_STAGED = 1 } rr_dns_method;
+rr_status rr_set_stage(rr_solver *s, int method, int rows, int stages);
+rr_status rr_get_stage(const rr_solver *s, int *method, int *rows, int *stages);
 
 #ifdef __cplusplus
 }

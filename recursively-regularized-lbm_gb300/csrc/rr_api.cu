@@ -6,6 +6,7 @@
 // runs); nothing synchronises until a readout or rr_sync().
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdarg>
@@ -216,6 +217,9 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st)
         else
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
                                    s->tile, st));
+    } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list) {
+        RR_CK(s->ops->staged(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
+                             s->frow_list, s->nfrows, s->stage_rows, s->stages, st, s->side, s->fork, s->join));
     } else if (s->p.lx >= 3) {
         RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
                            s->edge_list, s->nedges, s->rows_group, st));
@@ -277,7 +281,9 @@ size_t rr_bytes_for(const rr_params *p) {
     size_t b = 2 * (size_t)p->q * padded_stride(n) * elem + 256 + stat_doubles(*p) * sizeof(double);
     b += les_ubuf_bytes(*p);
     // edge-node list of the tile step (x-ends of the rows on a y/z wall face)
+    // and face-row list of the staged step
     if (p->lx >= 3) b += 2 * sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
+    if (rr::staged_ok(*p, elem)) b += sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
     return b;
 }
 
@@ -367,6 +373,32 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
             s->bytes += lb;
         }
     }
+    // the staged step's face rows (rows with y or z on a face, any kind), and
+    // its block shape: about 28 KB of populations per stage, two stages
+    if (rr::staged_ok(*p, s->ops->elem_bytes)) {
+        std::vector<uint32_t> frows;
+        for (int z = 0; z < p->lz; z++)
+            for (int y = 0; y < p->ly; y++)
+                if (y == 0 || y == p->ly - 1 || z == 0 || z == p->lz - 1) frows.push_back((uint32_t)z * p->ly + y);
+        const size_t lb = frows.size() * sizeof(uint32_t);
+        if (cudaMalloc(&s->frow_list, lb) != cudaSuccess) {
+            cudaGetLastError();
+            s->frow_list = nullptr;
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the face-row list"));
+        }
+        if (cudaMemcpy(s->frow_list, frows.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+            return cleanup(fail(RR_ERR_CUDA, "cannot upload the face-row list"));
+        s->nfrows = (uint32_t)frows.size();
+        s->bytes += lb;
+        if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(fail(RR_ERR_CUDA, "cannot create the face-row stream"));
+        const size_t row_bytes = (size_t)p->q * p->lx * s->ops->elem_bytes;
+        s->stage_rows = (int)std::max<size_t>(
+            1, std::min<size_t>({(28672 + row_bytes / 2) / row_bytes, (size_t)p->ly - 2, 32}));
+        s->stages = 2;
+    }
     // grids thinner than 3 nodes in x run the list-driven general step over
     // every node; all others the one-launch tile step
     if (p->lx < 3) {
@@ -402,6 +434,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     s->tile.zchunk = p->lz >= 64 ? 16 : (p->lz >= 16 ? 8 : p->lz);
     // launch shapes the autotuner found for this size class, if any
     rr::tuned_les_tile(*p, &s->tile);
+    if (s->frow_list) rr::tuned_stage(*p, &s->dns_method, &s->stage_rows, &s->stages);
     rr::tuned_rows_group(*p, &s->rows_group);
     *out = s;
     return RR_OK;
@@ -421,6 +454,13 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->all_list);
     cudaFree(s->edge_list);
     cudaFree(s->ubuf);
+    cudaFree(s->frow_list);
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
     if (s->home) cudaStreamDestroy(s->home);
     cudaGetLastError();
     delete s;

@@ -286,6 +286,10 @@ using TuneKey = std::tuple<int, int, int, int, int>; // q, storage, les, force, 
 std::mutex g_tune_mu;
 std::map<TuneKey, int> g_rows_group;
 std::map<TuneKey, rr::LesTile> g_les_tile;
+struct StageShape {
+    int method, rows, stages;
+};
+std::map<TuneKey, StageShape> g_stage;
 
 TuneKey tune_key(const rr_params &p) {
     const double n = (double)p.lx * p.ly * p.lz;
@@ -324,6 +328,16 @@ bool tuned_rows_group(const rr_params &p, int *rows_group) {
     auto it = g_rows_group.find(tune_key(p));
     if (it == g_rows_group.end()) return false;
     *rows_group = it->second;
+    return true;
+}
+
+bool tuned_stage(const rr_params &p, int *method, int *rows, int *stages) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_stage.find(tune_key(p));
+    if (it == g_stage.end()) return false;
+    *method = it->second.method;
+    *rows = it->second.rows;
+    *stages = it->second.stages;
     return true;
 }
 
@@ -583,6 +597,39 @@ rr_status rr_set_launch(rr_solver *s, int rows_group, const int *les_method, con
     return RR_OK;
 }
 
+rr_status rr_set_stage(rr_solver *s, int method, int rows, int stages) {
+    if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
+    if (method != RR_DNS_TILE && method != RR_DNS_STAGED)
+        return rr_internal_error(RR_ERR_INVALID, "method = %d unknown", method);
+    if (method == RR_DNS_STAGED) {
+        if (!s->frow_list)
+            return rr_internal_error(RR_ERR_INVALID, "the staged step needs a DNS grid of at least 3 nodes per axis "
+                                                     "with rows a multiple of 16 bytes");
+        const int rmax = std::min(32, s->p.ly - 2);
+        if (rows < 1 || rows > rmax || stages < 2 || stages > 4)
+            return rr_internal_error(RR_ERR_INVALID, "rows = %d (1 .. %d), stages = %d (2 .. 4)", rows, rmax, stages);
+        const size_t smem = 128 + (size_t)stages * s->p.q * rows * s->p.lx * s->ops->elem_bytes;
+        if (smem > 227 * 1024)
+            return rr_internal_error(RR_ERR_INVALID, "%d stages of %d rows need %zu bytes of shared memory (> 227 KB)",
+                                     stages, rows, smem);
+        s->stage_rows = rows;
+        s->stages = stages;
+    }
+    if (method != s->dns_method) {
+        s->dns_method = method;
+        rr::drop_graph(s);
+    }
+    return RR_OK;
+}
+
+rr_status rr_get_stage(const rr_solver *s, int *method, int *rows, int *stages) {
+    if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
+    if (method) *method = s->dns_method;
+    if (rows) *rows = s->stage_rows;
+    if (stages) *stages = s->stages;
+    return RR_OK;
+}
+
 rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run) {
     if (!s) return rr_internal_error(RR_ERR_INVALID, "solver is NULL");
     if (trial_steps < 1) return rr_internal_error(RR_ERR_INVALID, "trial_steps = %d", trial_steps);
@@ -622,7 +669,10 @@ rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run) {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_les_tile[tune_key(s->p)] = bt;
     } else if (rr::tile_step(s) || s->les_method == RR_LES_TWO_PASS) {
-        // the tile step, or the two tile passes of the WALE step: rows per group
+        // the tile step, or the two tile passes of the WALE step: rows per
+        // group; then (DNS) the staged step's block rows and stages
+        const int method0 = s->dns_method;
+        s->dns_method = RR_DNS_TILE;
         const int cands[3] = {32, 64, 128};
         float best = 1e30f;
         int br = s->rows_group;
@@ -636,8 +686,30 @@ rr_status rr_tune(rr_solver *s, int trial_steps, long long *steps_run) {
             }
         }
         s->rows_group = br;
+        StageShape bs{RR_DNS_TILE, s->stage_rows, s->stages};
+        if (s->frow_list) {
+            const int r0 = s->stage_rows;
+            const StageShape cs[4] = {{RR_DNS_STAGED, r0, 2}, {RR_DNS_STAGED, std::max(1, r0 / 2), 2},
+                                      {RR_DNS_STAGED, std::max(1, r0 / 2), 3}, {RR_DNS_STAGED, 2 * r0, 2}};
+            for (const StageShape &c : cs) {
+                if (rr_set_stage(s, c.method, c.rows, c.stages) != RR_OK) continue;
+                float ms = 0;
+                if ((st = time_steps(s->stream, [&] { return step(trial); }, &ms)) != RR_OK) return st;
+                if (ms < best) {
+                    best = ms;
+                    bs = c;
+                }
+            }
+        }
+        (void)method0;
+        if (bs.method == RR_DNS_STAGED) {
+            rr_set_stage(s, bs.method, bs.rows, bs.stages);
+        } else {
+            s->dns_method = RR_DNS_TILE;
+        }
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_rows_group[tune_key(s->p)] = br;
+        if (s->frow_list) g_stage[tune_key(s->p)] = StageShape{s->dns_method, s->stage_rows, s->stages};
     }
     rr::drop_graph(s);
     if (steps_run) *steps_run = run;

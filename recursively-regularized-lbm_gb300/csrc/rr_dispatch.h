@@ -35,6 +35,14 @@ struct Ops {
     cudaError_t (*tile)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const uint32_t *edges, uint32_t nedges,
                         int rows_group, cudaStream_t st);
+    // the staged step (needs nx * element size a multiple of 16): rows on a
+    // y/z face (frows) in one launch, the interior rows in blocks of R rows
+    // through an NS-stage shared-memory pipeline of bulk copies
+    // (side, fork, join: a second stream and two events for the face-row
+    // launch; side == NULL runs both launches on st)
+    cudaError_t (*staged)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
+                          const double F[3], int *status, const uint32_t *frows, uint32_t nfrows, int R, int NS,
+                          cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
     // the tile step's descriptor of one domain (TileArgs, written to out when
     // out != NULL) for a batch launch; returns its size, *nitems its warp items
     size_t (*tile_desc)(int q, const void *fin, void *fout, const Geom &g, double om1, const double F[3],

@@ -39,6 +39,12 @@ struct rr_solver {
     uint32_t nedges = 0;
     int block = 256;
     int rows_group = 32; // tile step: rows per work-item group (autotuned)
+    int dns_method = RR_DNS_TILE; // DNS step: tile step or staged step
+    int stage_rows = 2, stages = 3; // staged step: rows per block, pipeline stages
+    uint32_t *frow_list = nullptr;  // staged step: rows on a y or z face
+    uint32_t nfrows = 0;
+    cudaStream_t side = nullptr;     // staged step: the face-row launch, beside the interior one
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -50,6 +56,11 @@ namespace rr {
 bool has_force(const rr_params &p);
 // the step kind of a solver: the tile step (one launch, batchable) or not
 inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3; }
+// the staged step applies: DNS, at least 3 nodes on every axis, rows a
+// multiple of 16 bytes (bulk copies)
+inline bool staged_ok(const rr_params &p, size_t elem) {
+    return !p.use_les && p.lx >= 3 && p.ly >= 3 && p.lz >= 3 && ((size_t)p.lx * elem) % 16 == 0;
+}
 // one step of s from fin to fout on stream st (state bookkeeping is the caller's)
 rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st);
 // drop the solver's captured step graph (launch shapes or buffers changed)
@@ -57,6 +68,7 @@ void drop_graph(rr_solver *s);
 // tuned launch shapes of a size class, when the autotuner has seen it
 bool tuned_rows_group(const rr_params &p, int *rows_group);
 bool tuned_les_tile(const rr_params &p, LesTile *tile);
+bool tuned_stage(const rr_params &p, int *method, int *rows, int *stages);
 // detach s from its batch (the batch's work on s is finished first)
 rr_status batch_detach(rr_solver *s);
 

@@ -1,0 +1,327 @@
+// rr_stage.cuh -- the staged DNS step: interior rows through shared memory.
+//
+// Rows (row = z ny + y) with y in [1, ny-2] and z in [1, nz-2] are taken in
+// blocks of R consecutive rows of one z plane.  For population i the R
+// source rows of a block, (y0 - cy .. y0 - cy + R - 1, z - cz), are one
+// contiguous run of R nx values, so a block needs exactly Q bulk copies
+// (cp.async.bulk, global -> shared, completing on an mbarrier).  A persistent
+// CTA runs an S-stage pipeline: one thread issues the copies of the block S-1
+// ahead while all threads compute the current block from shared memory (the
+// x shift of a population is an index offset; a periodic x wraps inside the
+// row; a node on an x wall takes its entering populations from its own
+// post-collision values in global memory and applies the closure of that
+// face), then store their populations straight to global memory.  Rows on a
+// y or z face run in face_kernel, 32 nodes of one row per warp, through the
+// wrap-aware pull and the general face loop.  Each node gets the arithmetic
+// of the tile step, so the results are the same bit for bit.
+//
+// Every mbarrier wait is bounded: a wait that gives up sets bit 2 of the
+// watchdog word, the CTA stops taking blocks and its issuing thread waits
+// (bounded again) for the copies it still has in flight before it exits.
+#pragma once
+
+#include "rr_kernels.cuh"
+
+namespace rr {
+
+constexpr int STAGE_MAX = 4; // pipeline stages at most
+
+template <int Q, typename S>
+struct StageArgs {
+    const S *fin;
+    S *dst[Q];            // destination of node 0, per population
+    Geom g;
+    uint32_t nblocks;     // blocks of up to R interior rows
+    uint32_t rows;        // R
+    uint32_t yblocks;     // blocks per z plane
+    FastDiv div_yblocks, div_nxi; // div_nxi: nodes per row in the main loop (nx, or nx - 2 with x walls)
+    uint32_t stages;      // S (2 .. STAGE_MAX)
+    uint32_t stage_elems; // Q R nx
+    double om1;
+    double F[3];
+    int *status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// true once the phase with parity `parity` has completed; false after `limit`
+// unsuccessful polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit) {
+    const uint32_t a = smem_u32(bar);
+    for (uint32_t k = 0; k < limit; k++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// bytes (a multiple of 16) from global src to shared dst, completing on bar
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 24; // polls before a wait gives up
+
+// first row and row count of block b
+__device__ __forceinline__ void stage_block(uint32_t b, const FastDiv &div_yblocks, uint32_t yblocks, uint32_t R,
+                                            int ny, int &z, int &y0, int &rows) {
+    const uint32_t zp = fdiv(b, div_yblocks);
+    z = 1 + (int)zp;
+    y0 = 1 + (int)((b - zp * yblocks) * R);
+    rows = min((int)R, ny - 1 - y0);
+}
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256, 4) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
+    using T = typename CType<S>::T;
+    extern __shared__ __align__(128) unsigned char stage_smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(stage_smem);
+    S *buf = reinterpret_cast<S *>(stage_smem + 128);
+    __shared__ int s_fail;
+    const Geom &g = a.g;
+    const int nx = g.nx;
+    const uint32_t NS = a.stages;
+    const uint32_t R = a.rows;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+    }
+    __syncthreads();
+    // blocks of this CTA: blockIdx.x + k gridDim.x, k = 0 .. mine-1
+    const uint32_t mine = blockIdx.x < a.nblocks ? (a.nblocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    // the issuing thread: Q bulk copies of the CTA's k-th block into stage k % NS
+    auto issue = [&](uint32_t k) {
+        int z, y0, rows;
+        stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
+        const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
+        uint64_t *b = &bar[k % NS];
+        S *st = buf + (size_t)(k % NS) * a.stage_elems;
+        mbar_expect_tx(b, (uint32_t)LT::Q * bytes);
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const size_t src = (size_t)i * g.stride +
+                               ((size_t)(z - LT::cz(i)) * (size_t)g.ny + (size_t)(y0 - LT::cy(i))) * (size_t)nx;
+            bulk_g2s(st + (size_t)i * R * nx, a.fin + src, bytes, b);
+        });
+    };
+    uint32_t issued = 0, kfail = 0;
+    if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (; issued < mine && issued + 1 < NS; issued++) issue(issued);
+    }
+    const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    for (uint32_t k = 0; k < mine; k++) {
+        if (threadIdx.x == 0 && issued < mine) {
+            // stage (k + NS - 1) % NS was read in iteration k - 1, closed by its barrier
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(issued);
+            issued++;
+        }
+        const bool ok = mbar_wait(&bar[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                s_fail = 1;
+                kfail = k;
+                atomicOr(a.status, 4);
+            }
+            break;
+        }
+        int z, y0, rows;
+        stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
+        const S *st = buf + (size_t)(k % NS) * a.stage_elems;
+        // the main loop takes every node of the block's rows, or with x walls
+        // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
+        const bool xwall = g.face[0] != FACE_PERIODIC;
+        const int nxi = xwall ? nx - 2 : nx;
+        const int nmain = rows * nxi;
+        const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
+        const int total = ((nmain + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x + nwall;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            int r, x;
+            if (t < nmain) {
+                r = (int)fdiv((uint32_t)t, a.div_nxi);
+                x = (xwall ? 1 : 0) + t - r * nxi;
+            } else {
+                const int w = t - (total - nwall);
+                if (w < 0) continue;        // padding of the main loop's last round
+                r = w & 31;
+                if (r >= rows) continue;
+                x = w < 32 ? 0 : nx - 1;
+            }
+            const int y = y0 + r;
+            const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
+            const S *row = st + (size_t)r * nx;
+            T d[LT::Q];
+            if (x >= 1 && x <= nx - 2) {
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+                });
+            } else if (!xwall) {
+                // periodic x: the upstream node of an x-face node wraps inside the row
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    int xs = x - LT::cx(i);
+                    xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
+                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + xs);
+                });
+            } else {
+                // an x wall: the entering populations bounce back from this
+                // node's own post-collision values, then the face's closure
+                auto wall = [&](auto fc) {
+                    constexpr int F = decltype(fc)::value;
+                    constexpr uint32_t M = entering_mask<LT, F>();
+                    const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
+                    static_for<LT::Q>([&](auto ic) {
+                        constexpr int i = decltype(ic)::value;
+                        if constexpr (((M >> i) & 1u) != 0) {
+                            constexpr int o = LT::opp(i);
+                            const T v = ld_dev<T>(a.fin + (unsigned long long)o * g.stride + idx);
+                            d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+                        } else {
+                            d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+                        }
+                    });
+                    if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
+                };
+                if (x == 0) wall(std::integral_constant<int, 0>{});
+                else wall(std::integral_constant<int, 1>{});
+            }
+            Mom<T> m = moments<LT>(d);
+            T ux, uy, uz;
+            velocity(m, Fx, Fy, Fz, ux, uy, uz);
+            if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+            collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+            if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+                if (g.sround) {
+                    store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
+                    continue;
+                }
+            }
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                st_dev<T>(a.dst[i] + idx, d[i]);
+            });
+        }
+        __syncthreads(); // stage k % NS is free again
+    }
+    if (s_fail && threadIdx.x == 0) {
+        // copies still in flight target this CTA's shared memory: wait for
+        // them (blocks kfail .. issued-1, at most one per stage)
+        for (uint32_t k = kfail; k < issued; k++) mbar_wait(&bar[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT);
+    }
+}
+
+// rows on a y or z face (any kind): 32 consecutive nodes of one row per warp
+template <int Q, typename S>
+struct FaceArgs {
+    const S *fin;
+    S *dst[Q];
+    const S *src[Q]; // upstream addresses of the tile step (single-wall-face nodes)
+    Geom g;
+    const uint32_t *frows;
+    uint32_t nfrows, segs, nitems;
+    FastDiv div_segs, div_ny;
+    double om1;
+    double F[3];
+    int *status;
+};
+
+template <class LT, typename S, bool FORCE>
+__global__ void __launch_bounds__(256, 2) face_kernel(const __grid_constant__ FaceArgs<LT::Q, S> a) {
+    using T = typename CType<S>::T;
+    const uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (item >= a.nitems) return;
+    const Geom &g = a.g;
+    const uint32_t r = fdiv(item, a.div_segs);
+    const int x = (int)((item - r * a.segs) * 32u + lane);
+    if (x >= g.nx) return;
+    const uint32_t row = a.frows[r];
+    const int z = (int)fdiv(row, a.div_ny);
+    const int y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+    const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
+    const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    T d[LT::Q];
+    const bool xi = x >= 1 && x <= g.nx - 2, yi = y >= 1 && y <= g.ny - 2, zi = z >= 1 && z <= g.nz - 2;
+    const uint32_t faces = g.wallmask & ((x == 0 ? 1u : 0u) | (x == g.nx - 1 ? 2u : 0u) | (y == 0 ? 4u : 0u) |
+                                         (y == g.ny - 1 ? 8u : 0u) | (z == 0 ? 16u : 0u) |
+                                         (z == g.nz - 1 ? 32u : 0u));
+    // one wall face (y or z), interior on the other two axes
+    int wf = -1;
+    if (faces == 4u || faces == 8u) wf = (xi && zi) ? (faces == 4u ? 2 : 3) : -1;
+    else if (faces == 16u || faces == 32u) wf = (xi && yi) ? (faces == 16u ? 4 : 5) : -1;
+    switch (wf) {
+    case 2: wall_fast<LT, S, T, FORCE, 2>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+    case 3: wall_fast<LT, S, T, FORCE, 3>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+    case 4: wall_fast<LT, S, T, FORCE, 4>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+    case 5: wall_fast<LT, S, T, FORCE, 5>(a.src, a.fin, g, idx, d, Fx, Fy, Fz); break;
+    default:
+        // as the tile step: the wrap-aware pull, then one face's compiled
+        // closure or the general face loop
+        pull<LT>(a.fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
+        if (faces != 0u) {
+            if ((faces & (faces - 1u)) == 0u) {
+                switch (__ffs(faces) - 1) {
+                case 0: wall_face<LT, S, T, FORCE, 0>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 1: wall_face<LT, S, T, FORCE, 1>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 2: wall_face<LT, S, T, FORCE, 2>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 3: wall_face<LT, S, T, FORCE, 3>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                case 4: wall_face<LT, S, T, FORCE, 4>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                default: wall_face<LT, S, T, FORCE, 5>(a.fin, g, idx, d, Fx, Fy, Fz); break;
+                }
+            } else {
+                T tmp[LT::Q];
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    tmp[i] = d[i];
+                });
+                wall_multi<LT, S, T, FORCE>(a.fin, g, idx, x, y, z, Fx, Fy, Fz, tmp);
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    d[i] = tmp[i];
+                });
+            }
+        }
+        break;
+    }
+    Mom<T> m = moments<LT>(d);
+    T ux, uy, uz;
+    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+    if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+        if (g.sround) {
+            store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
+            return;
+        }
+    }
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        st_dev<T>(a.dst[i] + idx, d[i]);
+    });
+}
+
+} // namespace rr

@@ -100,6 +100,9 @@ def lib():
             "rr_batch_get_mode": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_batch_get_grouping": ([vp], ctypes.c_size_t),
             "rr_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+            "rr_set_stage": ([vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+            "rr_get_stage": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                              ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -265,6 +268,16 @@ class Solver:
         rg, m, t = ctypes.c_int(0), ctypes.c_int(0), (ctypes.c_int * 3)()
         _check(lib().rr_get_launch(self._h, ctypes.byref(rg), ctypes.byref(m), t))
         return rg.value, m.value, tuple(t)
+
+    def stage(self):
+        """(DNS method: 0 tile, 1 staged; rows per staged block; pipeline stages)"""
+        m, r, n = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().rr_get_stage(self._h, ctypes.byref(m), ctypes.byref(r), ctypes.byref(n)))
+        return m.value, r.value, n.value
+
+    def set_stage(self, method, rows=None, stages=None):
+        _, r, n = self.stage()
+        _check(lib().rr_set_stage(self._h, int(method), int(rows or r), int(stages or n)))
 
     def set_launch(self, rows_group, les_method=None, les_tile=None):
         m = None if les_method is None else ctypes.byref(ctypes.c_int(int(les_method)))
