@@ -52,6 +52,7 @@ WORKLOADS = {
     "cavity128_bf16": dict(kind="cavity", n=128, storage="bf16", Re=1000.0, U=0.1),
     "channel_les_f16": dict(kind="channel", storage="f16"),
     "tg100_f64": dict(kind="tg", storage="f64"),
+    "tg128_f16": dict(kind="tg128", storage="f16"),
 }
 BYTES_PER_POP = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}
 DTYPE = {"f64": "f64", "f32": "f32", "f16": "f16-store/f32-compute", "bf16": "bf16-store/f32-compute"}
@@ -64,6 +65,8 @@ def make(wl):
         return presets.cavity(n=w["n"], Re=w["Re"], U=w["U"], storage=w["storage"], variant="config")
     if w["kind"] == "channel":
         return presets.channel(storage=w["storage"], les=True, variant="config")
+    if w["kind"] == "tg128":
+        return presets.taylor_green(L=128, nz=128, tau=0.6, Ma=0.05, storage=w["storage"])
     return presets.taylor_green(L=100, nz=4, tau=0.6, Ma=0.01, storage=w["storage"])
 
 
@@ -75,7 +78,8 @@ def describe(wl, p, storage):
     if kind == "channel":
         return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 RR + WALE (C_w=0.5), Re_tau=180, walls y, periodic x/z, "
                 f"body force, {storage} storage")
-    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Ma=0.01, tau=0.6, periodic, {storage} storage"
+    ma = 0.05 if kind == "tg128" else 0.01
+    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Ma={ma}, tau=0.6, periodic, {storage} storage"
 
 
 def peaks():
@@ -207,6 +211,15 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def set_dns(s, how):
+    """the DNS step's method: tile (one launch of warp items), staged (shared-
+    memory pipeline of bulk copies) or tuned by rr_tune's choice for the class"""
+    if how == "tile":
+        s.set_stage(0)
+    elif how == "staged":
+        s.set_stage(1)
+
+
 def run_gpu(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -224,6 +237,11 @@ def run_gpu(args, rank, world, local_rank):
         import torch.distributed as tdist
 
     s = rrlbm.Solver(p)
+    set_dns(s, args.dns)
+    # rr kernel launches per step: tile step 1; staged step 2 (interior +
+    # face rows); WALE two-pass 2, fused 1
+    les_method, dns_method = s.launch()[1], s.stage()[0]
+    launches_per_step = (2 if les_method == 1 else 1) if p.use_les else (2 if dns_method == 1 else 1)
     s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
     stream = torch.cuda.ExternalStream(s.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -270,6 +288,7 @@ def run_gpu(args, rank, world, local_rank):
     pin = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in ("rho", "ux", "uy", "uz")}
     outs = {k: torch.empty((n,), dtype=torch.float64).pin_memory() for k in ("rho", "ux", "uy", "uz")}
     s2 = rrlbm.Solver(p)
+    set_dns(s2, args.dns)
     arr = {k: pin[k].numpy() for k in pin}
     s2.init_state(arr["rho"], arr["ux"], arr["uy"], arr["uz"])
     s2.step(W)
@@ -293,8 +312,6 @@ def run_gpu(args, rank, world, local_rank):
     if rank != 0:
         return
     pk, src = peaks()
-    # one launch per step: the tile step (DNS) or the WALE step (LES)
-    launches_per_step = 1
     bpl = 2 * q * BYTES_PER_POP[storage]
     achieved = n * bpl / (t_step * 1e-3) / 1e9
     traffic = ncu_traffic(args.workload)
@@ -468,6 +485,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="device-timed steps only (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--dns", default="tile", choices=["tile", "staged"],
+                    help="DNS step method of the single-domain lines (results are the same bit for bit)")
     ap.add_argument("--batch-domains", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=1000, help="0: skip the multi-domain line")
     ap.add_argument("--serve-requests", type=int, default=32, help="0: skip the serving line")

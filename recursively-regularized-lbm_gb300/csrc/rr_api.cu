@@ -376,10 +376,18 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     // the staged step's face rows (rows with y or z on a face, any kind), and
     // its block shape: about 28 KB of populations per stage, two stages
     if (rr::staged_ok(*p, s->ops->elem_bytes)) {
+        // grouped by the faces a row lies on (z-lo, z-hi, y-lo, y-hi, then the
+        // edge rows), so that neighbouring warps run the same compiled face path
         std::vector<uint32_t> frows;
+        std::vector<uint32_t> by_kind[5];
         for (int z = 0; z < p->lz; z++)
-            for (int y = 0; y < p->ly; y++)
-                if (y == 0 || y == p->ly - 1 || z == 0 || z == p->lz - 1) frows.push_back((uint32_t)z * p->ly + y);
+            for (int y = 0; y < p->ly; y++) {
+                const bool yf = y == 0 || y == p->ly - 1, zf = z == 0 || z == p->lz - 1;
+                if (!yf && !zf) continue;
+                const int kind = (yf && zf) ? 4 : zf ? (z == 0 ? 0 : 1) : (y == 0 ? 2 : 3);
+                by_kind[kind].push_back((uint32_t)z * p->ly + y);
+            }
+        for (auto &v : by_kind) frows.insert(frows.end(), v.begin(), v.end());
         const size_t lb = frows.size() * sizeof(uint32_t);
         if (cudaMalloc(&s->frow_list, lb) != cudaSuccess) {
             cudaGetLastError();

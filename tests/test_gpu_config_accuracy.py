@@ -1,0 +1,62 @@
+"""FP16/FP32-storage runs against FP64 runs at the workloads' own sizes.
+
+* Lid-driven cavity 128^3, Re = 1000, lid 0.1, 50,000 steps: centreline u(y)
+  and v(x) through the box centre, max and rms error relative to the lid
+  speed (bars: FP32 1e-4, FP16 2e-2).
+* WALE channel 384 x 192 x 128 (Re_tau = 180 formula, parabola + 10 % noise
+  start), 2,000 steps: plane-averaged streamwise velocity <u>(y), max error
+  relative to the centreline velocity (bar: 1 %).
+These are the long runs of the suite (about two minutes on one GPU)."""
+import numpy as np
+import pytest
+
+import rrlbm
+from rrlbm import presets
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+
+def _cavity(storage, n=128, steps=50000):
+    p, st = presets.cavity(n=n, Re=1000.0, U=0.1, storage=storage)
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
+        s.step(steps)
+        s.sync()
+        m = s.macro()
+    c = n // 2
+    return m["ux"][c, :, c], m["uy"][c, c, :]
+
+
+@pytest.fixture(scope="module")
+def cav128():
+    return _cavity("f64")
+
+
+@pytest.mark.parametrize("storage,bar", [("f32", 1e-4), ("f16", 2e-2)])
+def test_cavity128_centrelines_50k(storage, bar, cav128):
+    u64, v64 = cav128
+    u, v = _cavity(storage)
+    eu = np.abs(u - u64).max() / 0.1
+    ev = np.abs(v - v64).max() / 0.1
+    rms = np.sqrt(((u - u64) ** 2).mean() + ((v - v64) ** 2).mean()) / 0.1
+    print(f"\ncavity 128^3 Re=1000 50000 steps {storage}: max |du|/U = {eu:.2e}, max |dv|/U = {ev:.2e}, "
+          f"rms = {rms:.2e}; u_min = {u64.min():.5f}, v_max = {v64.max():.5f} (f64)")
+    assert max(eu, ev) < bar
+
+
+def _channel(storage, steps=2000):
+    p, st = presets.channel(les=True, storage=storage, variant="config")
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
+        s.step(steps)
+        s.sync()
+        prof, _ = s.profile()
+    return prof[:, 2], st["uc"]
+
+
+def test_channel_config_profile_f16():
+    u64, uc = _channel("f64")
+    u16, _ = _channel("f16")
+    err = np.abs(u16 - u64).max() / uc
+    print(f"\nWALE channel 384x192x128 2000 steps f16: max |<u>16 - <u>64| / U_c = {err:.2e}")
+    assert err < 1e-2
