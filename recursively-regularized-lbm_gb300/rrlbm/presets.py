@@ -199,6 +199,39 @@ def cavity(n=128, Re=1000.0, U=0.1, q=27, storage="f64", variant="config"):
     return p, st
 
 
+def laminar(storage="f64", q=27):
+    """The force-driven laminar channel of Laminar/*.f90: 60 x 20 x 2 nodes,
+    walls (bounce-back + regularized closure) at x = 1 and x = lx, periodic y
+    and z, body force in +y.  Rstar = 50, ustar = 0.05, nu = ustar nx / Rstar,
+    tau = 3 nu + 0.5, F_y = 8 nu ustar / nx^2 (Laminar/para.f90:33-39).  The
+    start is the rest equilibrium (initpop with u = 0) with the stored
+    velocity of the first macrovar, u_y = F_y / 2 (Laminar/main.f90:38-51),
+    which the first collision uses."""
+    nx, ny, nz = 60, 20, 2
+    Rstar, ustar = 50.0, 0.05
+    visc = ustar * nx / Rstar
+    p = params_default()
+    p.lx, p.ly, p.lz = nx, ny, nz
+    p.q = q
+    p.order = ORDER_CUDA if q == 27 else ORDER_FORTRAN
+    p.storage = STORAGE[storage]
+    p.use_les = 0
+    p.tau = 3.0 * visc + 0.5
+    p.force[0] = p.force[2] = 0.0
+    p.force[1] = 8.0 * visc * ustar / nx / nx
+    for f in range(6):
+        p.face[f] = FACE_PERIODIC
+        for a in range(3):
+            p.uwall[f][a] = 0.0
+    p.face[0] = p.face[1] = FACE_WALL
+    shp = (nz, ny, nx)
+    _, w = lattice(q)
+    f0 = np.ascontiguousarray(np.broadcast_to(w[:, None, None, None], (q,) + shp))
+    st = {"f": f0, "rho": np.ones(shp), "ux": np.zeros(shp), "uy": np.full(shp, 0.5 * p.force[1]),
+          "uz": np.zeros(shp), "ustar": ustar, "nu": visc}
+    return p, st
+
+
 def splitmix64(x):
     x = (x + np.uint64(0x9E3779B97F4A7C15)) & np.uint64(0xFFFFFFFFFFFFFFFF)
     x = ((x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & np.uint64(0xFFFFFFFFFFFFFFFF)

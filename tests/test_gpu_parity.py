@@ -222,3 +222,29 @@ def test_state_errors():
         s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
         with pytest.raises(rrlbm.RRError):
             s.macro()
+
+
+def test_laminar_channel_golden():
+    """The FP64 kernel against the reference's own output of the laminar
+    channel (Laminar/output/uy*.dat, mid-y line over x) and against the
+    oracle; same bar as the oracle's golden test."""
+    import os
+    from conftest import GOLDEN
+
+    p, st = presets.laminar()
+    o = oracle_for(p)
+    load_state(o, st)
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st["f"])
+        done = 0
+        for step in (5000, 10000, 60000):
+            s.step(step - done)
+            o.run(step - done)
+            done = step
+            m = s.macro()
+            ref = np.loadtxt(os.path.join(GOLDEN, f"laminar_uy{step}.txt"))
+            got = m["uy"][0, 10, :]
+            err = np.abs(got - ref).max() / np.abs(ref).max()
+            print(f"\nlaminar step {step}: GPU max |uy - ref| / max uy = {err:.2e}")
+            assert err < 1e-8, (step, err)
+            assert np.abs(m["uy"] - o.uy).max() / np.abs(ref).max() < 1e-11

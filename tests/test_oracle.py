@@ -119,3 +119,31 @@ def test_channel_matches_reference_live(les):
     assert np.array_equal(s.f, f)
     for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
         assert np.array_equal(getattr(s, k), a), k
+
+
+def _laminar_golden(step):
+    return np.loadtxt(os.path.join(GOLDEN, f"laminar_uy{step}.txt"))
+
+
+@pytest.mark.slow
+def test_laminar_channel_golden():
+    """The oracle against the reference's own FP64 output of the laminar
+    channel (Laminar/output/uy{5000,10000,60000}.dat, mid-y line over x).
+    The reference's wall closure takes its force term from the last node of
+    the collision sweep; in this flow (invariant in y and z, symmetric in x)
+    that term equals the local one, so agreement is to roundoff."""
+    from rrlbm import presets
+    from helpers import load_state, oracle_for
+
+    p, st = presets.laminar()
+    o = oracle_for(p)
+    load_state(o, st)
+    done = 0
+    for step in (5000, 10000, 60000):
+        o.run(step - done)
+        done = step
+        ref = _laminar_golden(step)
+        got = o.uy[0, 10, :]
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        print(f"laminar step {step}: max |uy - ref| / max uy = {err:.2e}")
+        assert err < 1e-8, (step, err)
