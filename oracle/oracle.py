@@ -41,7 +41,16 @@ class Params(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("lat", Lattice), ("tau", ctypes.c_double), ("force", ctypes.c_double * 3),
                 ("les", ctypes.c_int), ("cw", ctypes.c_double), ("face", ctypes.c_int * 6),
-                ("uwall", (ctypes.c_double * 3) * 6), ("tg_real4", ctypes.c_int)]
+                ("uwall", (ctypes.c_double * 3) * 6), ("tg_real4", ctypes.c_int),
+                ("ffield", ctypes.POINTER(ctypes.c_double))]
+
+
+class Trip(ctypes.Structure):
+    """orc_trip: the reference channel's start-up trip forcing"""
+    _fields_ = [("trip_steps", ctypes.c_int), ("istep", ctypes.c_longlong), ("phase", ctypes.c_double),
+                ("r", ctypes.c_int32 * 34), ("k", ctypes.c_int),
+                ("fx", ctypes.POINTER(ctypes.c_double)), ("fy", ctypes.POINTER(ctypes.c_double)),
+                ("fz", ctypes.POINTER(ctypes.c_double))]
 
 
 class _State(ctypes.Structure):
@@ -76,6 +85,12 @@ def lib():
         L.orc_feq.argtypes = [ctypes.POINTER(Lattice), ctypes.c_int] + [ctypes.c_double] * 4
         L.orc_feq.restype = ctypes.c_double
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_srand.argtypes = [ctypes.POINTER(Trip), ctypes.c_uint]
+        L.orc_rand.argtypes = [ctypes.POINTER(Trip)]
+        L.orc_rand.restype = ctypes.c_int
+        L.orc_trip_force.argtypes = [ctypes.POINTER(Params), ctypes.c_longlong, ctypes.c_double, dp, dp, dp]
+        L.orc_run_trip.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_State), ctypes.POINTER(Trip),
+                                   ctypes.c_int]
         _LIB = L
     return _LIB
 
@@ -120,6 +135,19 @@ class Sim:
         self.uz = np.zeros_like(self.ux)
         self.taut = np.zeros_like(self.ux)
         self.n = n
+        self.trip = None
+
+    def enable_trip(self, trip_steps=50000, istep=0, seed=12345):
+        """the channel program's trip forcing for steps < trip_steps, the run
+        starting after step istep (the rand() sequence restarts with the run)"""
+        T = Trip()
+        T.trip_steps = int(trip_steps)
+        T.istep = int(istep)
+        T.phase = 0.0
+        lib().orc_srand(ctypes.byref(T), int(seed))
+        self.ffield = np.zeros((3,) + self.shape)
+        T.fx, T.fy, T.fz = _p(self.ffield[0]), _p(self.ffield[1]), _p(self.ffield[2])
+        self.trip = T
 
     # -- initial states -------------------------------------------------
     def init_tg_reference(self, U0):
@@ -151,7 +179,10 @@ class Sim:
 
     def run(self, nsteps):
         s = self._state()
-        lib().orc_run(ctypes.byref(self.P), ctypes.byref(s), int(nsteps))
+        if self.trip is not None:
+            lib().orc_run_trip(ctypes.byref(self.P), ctypes.byref(s), ctypes.byref(self.trip), int(nsteps))
+        else:
+            lib().orc_run(ctypes.byref(self.P), ctypes.byref(s), int(nsteps))
         # the C side swaps f/ftmp each step; follow its pointers
         if ctypes.addressof(s.f.contents) != self.f.ctypes.data:
             self.f, self.ftmp = self.ftmp, self.f

@@ -10,6 +10,7 @@
  */
 #include "LBMLES.h"
 
+#include <stdlib.h>
 #include <string.h>
 
 thread_local uint3 threadIdx;
@@ -111,5 +112,37 @@ void ref_step(double *f, double *f_temp, double *rho, double *ux, double *uy, do
 void ref_run(int nsteps, double *f, double *f_temp, double *rho, double *ux, double *uy,
              double *uz, double *fx, double *fy, double *fz, double *taut) {
     for (int i = 0; i < nsteps; i++) ref_step(f, f_temp, rho, ux, uy, uz, fx, fy, fz, taut);
+}
+
+/* the loop of main.cu:29-46 with the trip forcing: srand(12345) at the start
+ * of the run, then for each step n < npforcing the phase redrawn with
+ * rand() / RAND_MAX when n % 2000 == 0 and forcing_GP; forcing after */
+void ref_run_trip(int nsteps, long long start_istep, int npforcing, double *f, double *f_temp, double *rho,
+                  double *ux, double *uy, double *uz, double *fx, double *fy, double *fz, double *taut) {
+    srand(12345);
+    for (long long n = start_istep + 1; n <= start_istep + nsteps; n++) {
+        if (n < npforcing) {
+            d_istep = (int)n;
+            if (n % 2000 == 0) d_rand_phase = (double)rand() / RAND_MAX;
+            launch([&] { forcing_GP(fx, fy, fz); });
+        } else {
+            launch([&] { forcing(fx, fy, fz); });
+        }
+        d_istep = 1; /* collision_RR prints every 1000 steps otherwise */
+        if (USE_LES) launch([&] { LES_WALE(ux, uy, uz, taut); });
+        launch([&] { collision_RR(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+        launch([&] { streaming(f, f_temp); });
+        launch([&] { BB(f, f_temp); });
+        memcpy(f, f_temp, sizeof(double) * (size_t)NPOP * LXYZ);
+        launch([&] { macrovar(f, fx, fy, fz, rho, ux, uy, uz); });
+        launch([&] { RRBC(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+        launch([&] { macrovar_BN(f, fx, fy, fz, rho, ux, uy, uz); });
+    }
+}
+
+/* rand() of this C library after srand(seed), n values (checks of the restatement) */
+void ref_rand(unsigned seed, int n, int *out) {
+    srand(seed);
+    for (int i = 0; i < n; i++) out[i] = rand();
 }
 }

@@ -365,6 +365,19 @@ void orc_regularize_node(const orc_lattice *L, const double F[3], double *f,
 
 static inline int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+/* the body force at node idx: the per-node field when there is one */
+static inline void node_force(const orc_params *P, long N, long idx, double F[3]) {
+    if (P->ffield) {
+        F[0] = P->ffield[idx];
+        F[1] = P->ffield[N + idx];
+        F[2] = P->ffield[2 * N + idx];
+    } else {
+        F[0] = P->force[0];
+        F[1] = P->force[1];
+        F[2] = P->force[2];
+    }
+}
+
 /* stream (pull form of streaming.cu:3-24 / D3Q27RR.f90:400-419), then the wall
  * faces in the order x-lo, x-hi, y-lo, y-hi, z-lo, z-hi: half-way bounce-back
  * from the post-collision value of the opposite population at the same node
@@ -404,7 +417,11 @@ void orc_stream_walls(const orc_params *P, const double *fin, double *fout) {
                         }
                         fl[ip] = v;
                     }
-                    if (P->face[face] == ORC_FACE_WALL) orc_regularize_node(L, P->force, fl, entering);
+                    if (P->face[face] == ORC_FACE_WALL) {
+                        double Fn[3];
+                        node_force(P, N, idx, Fn);
+                        orc_regularize_node(L, Fn, fl, entering);
+                    }
                 }
                 for (int ip = 0; ip < q; ip++) fout[ip * N + idx] = fl[ip];
             }
@@ -419,7 +436,9 @@ void orc_moments_all(const orc_params *P, const double *f, double *rho, double *
     for (long idx = 0; idx < N; idx++) {
         double fl[27];
         for (int ip = 0; ip < L->q; ip++) fl[ip] = f[ip * N + idx];
-        orc_moments_node(L, P->force, fl, &rho[idx], &ux[idx], &uy[idx], &uz[idx]);
+        double Fn[3];
+        node_force(P, N, idx, Fn);
+        orc_moments_node(L, Fn, fl, &rho[idx], &ux[idx], &uy[idx], &uz[idx]);
     }
 }
 
@@ -437,8 +456,11 @@ void orc_collide_all(const orc_params *P, double *f, const double *rho, const do
         double tau_eff = P->les ? P->tau + taut[idx] : P->tau;
         if (P->tg_real4)
             collide_node_tg4(L, &T, tau_eff, rho[idx], ux[idx], uy[idx], uz[idx], fl);
-        else
-            orc_collide_node(L, tau_eff, P->force, rho[idx], ux[idx], uy[idx], uz[idx], fl);
+        else {
+            double Fn[3];
+            node_force(P, N, idx, Fn);
+            orc_collide_node(L, tau_eff, Fn, rho[idx], ux[idx], uy[idx], uz[idx], fl);
+        }
         for (int ip = 0; ip < L->q; ip++) f[ip * N + idx] = fl[ip];
     }
 }
@@ -527,6 +549,89 @@ void orc_step(const orc_params *P, orc_state *S) {
 
 void orc_run(const orc_params *P, orc_state *S, int nsteps) {
     for (int i = 0; i < nsteps; i++) orc_step(P, S);
+}
+
+void orc_srand(orc_trip *T, unsigned seed) {
+    int32_t r[344];
+    r[0] = (int32_t)seed;
+    for (int i = 1; i < 31; i++) {
+        long long w = (16807LL * (long long)r[i - 1]) % 2147483647LL;
+        if (w < 0) w += 2147483647LL;
+        r[i] = (int32_t)w;
+    }
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    for (int i = 34; i < 344; i++) r[i] = (int32_t)((uint32_t)r[i - 31] + (uint32_t)r[i - 3]);
+    for (int i = 0; i < 34; i++) T->r[i] = r[310 + i];
+    T->k = 0; /* r[k] holds term i - 34 of the next term i */
+}
+
+int orc_rand(orc_trip *T) {
+    /* ring of the last 34 terms: oldest at k; term i-31 is at k+3, i-3 at k+31 */
+    const int32_t v = (int32_t)((uint32_t)T->r[(T->k + 3) % 34] + (uint32_t)T->r[(T->k + 31) % 34]);
+    T->r[T->k] = v;
+    T->k = (T->k + 1) % 34;
+    return (int)((uint32_t)v >> 1);
+}
+
+/* forcing_GP of macrovar.cu:76-115, written in the same operation order so
+ * that it rounds as the reference does (integer divisions included:
+ * LY / 4, and ix / LX, which is 0 inside the domain) */
+void orc_trip_force(const orc_params *P, long long n, double phase, double *fx, double *fy, double *fz) {
+    const int LX = P->nx, LY = P->ny, LZ = P->nz;
+    const double pi2 = 2 * acos(-1.0);
+    const double Tpd = 2000.0;
+    const double LYq = LY / 4;
+    const int h0 = 2;
+    const double beta9 = 3.0, gamma9 = 2.0;
+    const double F0 = P->force[0];
+    const double Amp0 = (100.0 * beta9 / LY) * sin(pi2 * (double)n / Tpd);
+#pragma omp parallel for schedule(static)
+    for (int iz = 0; iz < LZ; iz++)
+        for (int iy = 0; iy < LY; iy++)
+            for (int ix = 0; ix < LX; ix++) {
+                const long idx = ((long)iz * LY + iy) * LX + ix;
+                double x = F0, y = 0.0, z = 0.0;
+                if (iy > h0 && iy < LYq + h0) {
+                    x = F0 * (1.0 - Amp0 * LX / beta9 * sin(pi2 * (iy - h0) / LYq) * sin(beta9 * pi2 * ix / LX) *
+                                        cos(gamma9 * pi2 * iz / LZ));
+                    y = F0 * Amp0 * 0.5 * LYq * (1 - cos(pi2 * (iy - h0) / LYq)) * cos(beta9 * pi2 * ix / LX) *
+                        cos(gamma9 * pi2 * iz / LZ);
+                    z = F0 * Amp0 * 0.5 * LZ / gamma9 * sin(pi2 * (iy - h0) / LYq) * cos(beta9 * pi2 * ix / LX) *
+                        sin(gamma9 * pi2 * iz / LZ);
+                } else if (iy > 0.75 * LY - h0 && iy < LY - h0) {
+                    x = F0 * (1.0 + Amp0 * LX / beta9 * sin(pi2 * (-LY + iy + h0 + LYq) / LYq) *
+                                        sin(beta9 * pi2 * (ix / LX + phase)) * cos(gamma9 * pi2 * iz / LZ));
+                    y = -F0 * Amp0 * 0.5 * LYq * (1 - cos(pi2 * (-LY + iy + h0 + LYq) / LYq)) *
+                        cos(beta9 * pi2 * (ix / LX + phase)) * cos(gamma9 * pi2 * iz / LZ);
+                    z = -F0 * Amp0 * 0.5 * LZ / gamma9 * sin(pi2 * (-LY + iy + h0 + LYq) / LYq) *
+                        cos(beta9 * pi2 * (ix / LX + phase)) * sin(gamma9 * pi2 * iz / LZ);
+                }
+                fx[idx] = x;
+                fy[idx] = y;
+                fz[idx] = z;
+            }
+}
+
+void orc_run_trip(const orc_params *P, orc_state *S, orc_trip *T, int nsteps) {
+    const long N = (long)P->nx * P->ny * P->nz;
+    orc_params Q = *P;
+    for (int i = 0; i < nsteps; i++) {
+        const long long n = T->istep + 1;
+        if (n < T->trip_steps) {
+            if (n % 2000 == 0) T->phase = (double)orc_rand(T) / 2147483647.0;
+            orc_trip_force(P, n, T->phase, T->fx, T->fy, T->fz);
+        } else {
+            for (long idx = 0; idx < N; idx++) {
+                T->fx[idx] = P->force[0];
+                T->fy[idx] = 0.0;
+                T->fz[idx] = 0.0;
+            }
+        }
+        /* the field is contiguous: fx, fy, fz of length N each */
+        Q.ffield = T->fx;
+        orc_step(&Q, S);
+        T->istep = n;
+    }
 }
 
 /* ------------------------------------------------------------------------ */

@@ -66,6 +66,9 @@ typedef struct {
      * collision and the start state round them to single precision as that
      * program does; populations, moments and weights stay REAL(8). */
     int tg_real4;
+    /* per-node body force (fx, fy, fz: three arrays of nx ny nz), or NULL
+     * for the uniform force above */
+    const double *ffield;
 } orc_params;
 
 /* State in the reference's own form: populations after streaming and wall
@@ -92,6 +95,33 @@ void orc_moments_node(const orc_lattice *L, const double F[3], const double *f, 
 /* one full reference time step on the whole grid */
 void orc_step(const orc_params *P, orc_state *S);
 void orc_run(const orc_params *P, orc_state *S, int nsteps);
+
+/* The channel program's start-up "GP" trip forcing (macrovar.cu:76-115,
+ * main.cu:29-46): for steps n < trip_steps the body force is a spatial field
+ * of n and of a phase redrawn from the C library's rand() every 2000 steps
+ * (srand(12345) at the start of the run, phase 0 before the first draw);
+ * from trip_steps on it is the uniform force.  The field's force_in_x is the
+ * x component of orc_params.force. */
+typedef struct {
+    int trip_steps;        /* the reference's npforcing (50000) */
+    long long istep;       /* steps done */
+    double phase;          /* d_rand_phase */
+    int32_t r[34];         /* rand() state: the last 34 terms of its sequence */
+    int k;                 /* next slot of r */
+    double *fx, *fy, *fz;  /* the force arrays of the current step (caller-owned) */
+} orc_trip;
+
+/* the C library's rand() after srand(seed): the additive-feedback generator
+ * r_i = r_{i-3} + r_{i-31} (mod 2^32), output r_i >> 1, seeded by
+ * r_0 = seed, r_i = 16807 r_{i-1} mod (2^31 - 1) (i < 31), r_i = r_{i-31}
+ * (31 <= i < 34), with the first 310 outputs discarded */
+void orc_srand(orc_trip *T, unsigned seed);
+int orc_rand(orc_trip *T);
+/* the force field of step n with phase `phase` into fx, fy, fz */
+void orc_trip_force(const orc_params *P, long long n, double phase, double *fx, double *fy, double *fz);
+/* nsteps steps with the trip forcing: T->istep advances; before step n the
+ * phase is redrawn when n % 2000 == 0 and n < trip_steps */
+void orc_run_trip(const orc_params *P, orc_state *S, orc_trip *T, int nsteps);
 
 /* WALE eddy viscosity (LES.cu:4-98), generalised to walls on any face */
 void orc_wale(const orc_params *P, const double *ux, const double *uy, const double *uz,

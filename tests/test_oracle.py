@@ -147,3 +147,37 @@ def test_laminar_channel_golden():
         err = np.abs(got - ref).max() / np.abs(ref).max()
         print(f"laminar step {step}: max |uy - ref| / max uy = {err:.2e}")
         assert err < 1e-8, (step, err)
+
+
+def test_rand_restatement_matches_c_library():
+    """orc_rand (the C library's additive-feedback rand(), restated) against
+    the C library itself after srand(12345), the reference's seed"""
+    libc = ctypes.CDLL(None)
+    libc.srand(12345)
+    want = [libc.rand() for _ in range(5000)]
+    T = O.Trip()
+    O.lib().orc_srand(ctypes.byref(T), 12345)
+    got = [O.lib().orc_rand(ctypes.byref(T)) for _ in range(5000)]
+    assert got == want
+
+
+@pytest.mark.parametrize("les", [0, 1])
+def test_trip_forcing_matches_reference_live(les):
+    """The start-up trip forcing (forcing_GP with the rand() phase, main.cu:29-46)
+    of the oracle against the reference's own kernels, bit for bit, across two
+    phase draws (steps 2000 and 4000) and the switch to the uniform force."""
+    R = _ref_lib(les)
+    R.ref_run_trip.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_int] + [ctypes.c_void_p] * 10
+    npforcing, steps = 4050, 4100
+    s = _channel_sim(les, R.ref_tau(), R.ref_force_in_x())
+    s.init_channel_loglaw(R.ref_ustar(), R.ref_ystar())
+    s.enable_trip(npforcing)
+    f, rho, ux, uy, uz = (a.copy() for a in (s.f, s.rho, s.ux, s.uy, s.uz))
+    ft, fx, fy, fz, taut = (np.zeros_like(a) for a in (f, rho, rho, rho, rho))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    R.ref_run_trip(steps, 0, npforcing, P(f), P(ft), P(rho), P(ux), P(uy), P(uz), P(fx), P(fy), P(fz), P(taut))
+    s.run(steps)
+    assert s.trip.istep == steps
+    assert np.array_equal(s.f, f)
+    for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
+        assert np.array_equal(getattr(s, k), a), k
