@@ -89,6 +89,14 @@ typedef struct rr_params {
     int device;          /* CUDA device ordinal */
     double ustar, ystar; /* friction velocity and viscous length, for output_profile's y+ */
     int rounding;        /* rr_rounding of FP16/BF16 stores (default stochastic) */
+    /* start-up trip forcing of the channel program (forcing_GP,
+     * macrovar.cu:76-115; main.cu:29-46): for time steps n < trip_steps the
+     * body force is its spatial field of n and of a phase redrawn from the C
+     * library's rand() sequence (srand(12345) at the start of the run) every
+     * 2000 steps, with force[0] as force_in_x; from trip_steps on the uniform
+     * force.  0 (default): off; the reference's value is 50000.  D3Q27 and
+     * lx >= 3 only; steps in the trip phase run without CUDA graphs. */
+    int trip_steps;
 } rr_params;
 
 typedef struct rr_solver rr_solver;
@@ -165,6 +173,12 @@ rr_status rr_get_accum(rr_solver *s, double *sums, long long *samples);
 /* The reference's file outputs, byte-compatible (what = RR_OUT_* bits),
  * written under directory dir with istep = rr_get_istep(). */
 rr_status rr_output(rr_solver *s, unsigned what, const char *dir);
+
+/* The body force of the step the readouts show (the reference's
+ * d_force_realx/y/z, LBMLES.h:46-50, written by forcing / forcing_GP):
+ * fx, fy, fz of n values each, consecutively in out (3 n doubles), on the
+ * host or the device.  The uniform force outside the trip-forcing phase. */
+rr_status rr_get_force(rr_solver *s, double *out, int where);
 
 /* Restart files in the reference's format (output_flow + output_f, read
  * back by initialize() with CONTINUE_STEP, initial.cu:189-265):

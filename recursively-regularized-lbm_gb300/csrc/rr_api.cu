@@ -96,6 +96,9 @@ rr_status validate(const rr_params *p) {
     if (p->use_les && !(p->cw >= 0.0)) return fail(RR_ERR_INVALID, "cw = %g", p->cw);
     if (p->rounding != RR_ROUND_NEAREST && p->rounding != RR_ROUND_STOCHASTIC)
         return fail(RR_ERR_INVALID, "rounding = %d unknown", p->rounding);
+    if (p->trip_steps < 0) return fail(RR_ERR_INVALID, "trip_steps = %d", p->trip_steps);
+    if (p->trip_steps > 0 && (p->q != 27 || p->lx < 3))
+        return fail(RR_ERR_UNSUPPORTED, "trip forcing needs D3Q27 and lx >= 3");
     return RR_OK;
 }
 
@@ -134,6 +137,12 @@ rr_status set_device(const rr_solver *s) {
     return RR_OK;
 }
 
+// the force field of the state a readout shows (step istep), while the trip
+// forcing has made it a field
+const double *readout_field(rr_solver *s) {
+    return (s->ffield && s->istep >= 1 && s->istep < s->p.trip_steps) ? rr::trip_slot(s, s->istep) : nullptr;
+}
+
 // rho, u (and taut) of the current state into aux
 rr_status readout_macros(rr_solver *s, bool want_taut) {
     rr_status st = ensure_aux(s);
@@ -142,7 +151,7 @@ rr_status readout_macros(rr_solver *s, bool want_taut) {
     double *rho = s->aux, *ux = rho + n, *uy = ux + n, *uz = uy + n, *tt = uz + n;
     // the previous buffer holds the post-collision state the last step read
     RR_CK(s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, nullptr, 0,
-                          s->pos, rho, ux, uy, uz, s->stream));
+                          s->pos, rho, ux, uy, uz, readout_field(s), s->stream));
     if (want_taut) RR_CK(rr::launch_wale(s->g, s->p.cw, ux, uy, uz, tt, s->stream));
     return RR_OK;
 }
@@ -157,7 +166,7 @@ rr_status copy_out(rr_solver *s, double *dst, const double *src, size_t count, i
 
 rr_status launch_steps(rr_solver *s, int n) {
     for (int k = 0; k < n; k++) {
-        rr_status st = rr::launch_one(s, s->buf[s->cur], s->buf[1 - s->cur], s->stream);
+        rr_status st = rr::launch_one(s, s->buf[s->cur], s->buf[1 - s->cur], s->stream, s->istep + k);
         if (st != RR_OK) return st;
         s->cur = 1 - s->cur;
     }
@@ -208,21 +217,47 @@ namespace rr {
 
 bool has_force(const rr_params &p) { return p.force[0] != 0.0 || p.force[1] != 0.0 || p.force[2] != 0.0; }
 
-rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st) {
+// the force-field slot of step n
+double *trip_slot(rr_solver *s, long long n) { return s->ffield + (size_t)(n & 1) * 3 * s->g.stride; }
+
+// the force of step n into its slot: the trip field while n < trip_steps
+// (redrawing the phase every 2000 steps), the uniform force after
+rr_status trip_prepare(rr_solver *s, long long n, cudaStream_t st) {
+    const int trip = n < s->p.trip_steps ? 1 : 0;
+    double amp = 0.0;
+    if (trip) {
+        if (n % 2000 == 0) s->trip_phase = (double)s->trip_rng.next() / 2147483647.0;
+        amp = (100.0 * 3.0 / s->p.ly) * sin(2 * acos(-1.0) * (double)n / 2000.0);
+    }
+    RR_CK(rr::launch_trip_force(trip_slot(s, n), s->g.stride, s->p.lx, s->p.ly, s->p.lz, trip, amp,
+                                s->trip_phase, s->p.force, st));
+    return RR_OK;
+}
+
+rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st, long long i) {
     const bool force = rr::has_force(s->p);
+    // in the trip phase: the force of step i+1 (walls and moments) and of
+    // step i+2 (the collision), per node
+    const double *ffp = nullptr, *ffc = nullptr;
+    if (trip_phase(s, i)) {
+        rr_status ts = trip_prepare(s, i + 2, st);
+        if (ts != RR_OK) return ts;
+        ffp = trip_slot(s, i + 1);
+        ffc = trip_slot(s, i + 2);
+    }
     if (s->p.use_les) {
-        if (s->les_method == RR_LES_TWO_PASS && s->ubuf)
+        if ((s->les_method == RR_LES_TWO_PASS || ffp) && s->ubuf)
             RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
-                               s->edge_list, s->nedges, s->rows_group, s->ubuf, st));
+                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, st));
         else
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
                                    s->tile, st));
-    } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list) {
+    } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list && !ffp) {
         RR_CK(s->ops->staged(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
                              s->frow_list, s->nfrows, s->stage_rows, s->stages, st, s->side, s->fork, s->join));
     } else if (s->p.lx >= 3) {
         RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
-                           s->edge_list, s->nedges, s->rows_group, st));
+                           s->edge_list, s->nedges, s->rows_group, ffp, ffc, st));
     } else {
         RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status, s->all,
                            s->block, st));
@@ -284,6 +319,7 @@ size_t rr_bytes_for(const rr_params *p) {
     // and face-row list of the staged step
     if (p->lx >= 3) b += 2 * sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
     if (rr::staged_ok(*p, elem)) b += sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
+    if (p->trip_steps > 0) b += 6 * padded_stride(n) * sizeof(double);
     return b;
 }
 
@@ -436,6 +472,15 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     } else {
         s->les_method = RR_LES_FUSED;
     }
+    if (p->trip_steps > 0) {
+        const size_t fb = 6 * (size_t)g.stride * sizeof(double);
+        if (cudaMalloc(&s->ffield, fb) != cudaSuccess) {
+            cudaGetLastError();
+            s->ffield = nullptr;
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of trip force fields", fb));
+        }
+        s->bytes += fb;
+    }
     // LES tile by size class: full 32-wide rows when x allows, else 16
     s->tile.tx = p->lx >= 32 ? 32 : 16;
     s->tile.ty = 256 / s->tile.tx;
@@ -463,6 +508,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->edge_list);
     cudaFree(s->ubuf);
     cudaFree(s->frow_list);
+    cudaFree(s->ffield);
     if (s->side) {
         cudaStreamSynchronize(s->side);
         cudaStreamDestroy(s->side);
@@ -475,8 +521,11 @@ rr_status rr_destroy(rr_solver *s) {
     return RR_OK;
 }
 
-rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const double *ux,
-                        const double *uy, const double *uz, int where) {
+namespace {
+
+// the state upload of a run that starts after step istep0 (0, or a restart)
+rr_status init_state_at(rr_solver *s, const double *f, const double *rho, const double *ux, const double *uy,
+                        const double *uz, int where, long long istep0) {
     if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
     if (!rho || !ux || !uy || !uz) return fail(RR_ERR_INVALID, "rho, ux, uy, uz are required");
     if (s->batch) return fail(RR_ERR_STATE, "the solver is a member of a batch: remove it to set its state");
@@ -497,9 +546,24 @@ rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const 
     if (e == cudaSuccess && f) e = cudaMemcpyAsync(d_f, f, nf * sizeof(double), kind, s->stream);
     // the reference's first step computes tau_t from these macros (main.cu:375-379)
     if (e == cudaSuccess && s->p.use_les) e = rr::launch_wale(s->g, s->p.cw, d_ux, d_uy, d_uz, d_tt, s->stream);
+    // the trip forcing restarts with the run: srand(12345), phase 0; the
+    // first collision (step istep0 + 1) takes that step's force
+    const double *ff = nullptr;
+    if (e == cudaSuccess && s->ffield) {
+        s->trip_rng.seed(12345);
+        s->trip_phase = 0.0;
+        if (istep0 + 1 < s->p.trip_steps) {
+            rr_status ts = rr::trip_prepare(s, istep0 + 1, s->stream);
+            if (ts != RR_OK) {
+                cudaFreeAsync(tmp, s->stream);
+                return ts;
+            }
+            ff = rr::trip_slot(s, istep0 + 1);
+        }
+    }
     if (e == cudaSuccess)
         e = s->ops->upload(s->p.q, rr::has_force(s->p), s->buf[0], s->g, s->p.tau, s->p.force, d_f, n,
-                           s->pos, d_rho, d_ux, d_uy, d_uz, s->p.use_les ? d_tt : nullptr, s->stream);
+                           s->pos, d_rho, d_ux, d_uy, d_uz, s->p.use_les ? d_tt : nullptr, ff, s->stream);
     cudaError_t e2 = cudaFreeAsync(tmp, s->stream);
     if (e != cudaSuccess) return fail(RR_ERR_CUDA, "state upload failed: %s", cudaGetErrorString(e));
     if (e2 != cudaSuccess) return fail(RR_ERR_CUDA, "cudaFreeAsync: %s", cudaGetErrorString(e2));
@@ -507,12 +571,19 @@ rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const 
     // "previous buffer" (its own input for readouts) is buffer 1, which gets the
     // same role after the first rr_step.  Until then readouts are of the input.
     s->cur = 0;
-    s->istep = 0;
+    s->istep = istep0;
     s->ready = true;
     s->stepped = false;
     RR_CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
     if (where == RR_HOST) RR_CK(cudaStreamSynchronize(s->stream));
     return RR_OK;
+}
+
+} // namespace
+
+rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const double *ux,
+                        const double *uy, const double *uz, int where) {
+    return init_state_at(s, f, rho, ux, uy, uz, where, 0);
 }
 
 rr_status rr_step(rr_solver *s, int nsteps) {
@@ -522,6 +593,15 @@ rr_status rr_step(rr_solver *s, int nsteps) {
     if (s->batch) return fail(RR_ERR_STATE, "the solver is a member of a batch: step it with rr_batch_step");
     if (set_device(s) != RR_OK) return RR_ERR_CUDA;
     int left = nsteps;
+    // steps of the trip phase: single launches, each with its force fields
+    while (left > 0 && rr::trip_phase(s, s->istep)) {
+        rr_status st = launch_steps(s, 1);
+        if (st != RR_OK) return st;
+        s->istep++;
+        s->stepped = true;
+        left--;
+    }
+    const int rest = left;
     if (left >= 2 * GRAPH_STEPS) {
         if (s->cur != 0) {
             rr_status st = launch_steps(s, 1);
@@ -537,8 +617,8 @@ rr_status rr_step(rr_solver *s, int nsteps) {
     }
     rr_status st = launch_steps(s, left);
     if (st != RR_OK) return st;
-    s->istep += nsteps;
-    if (nsteps > 0) s->stepped = true;
+    s->istep += rest;
+    if (rest > 0) s->stepped = true;
     return RR_OK;
 }
 
@@ -586,7 +666,7 @@ rr_status rr_get_f(rr_solver *s, double *f, int where) {
         dst = tmp;
     }
     cudaError_t e = s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, dst,
-                                    n, s->pos, nullptr, nullptr, nullptr, nullptr, s->stream);
+                                    n, s->pos, nullptr, nullptr, nullptr, nullptr, readout_field(s), s->stream);
     if (e == cudaSuccess && tmp) e = cudaMemcpyAsync(f, tmp, nf * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
     if (tmp) cudaFreeAsync(tmp, s->stream);
     if (e != cudaSuccess) return fail(RR_ERR_CUDA, "readout failed: %s", cudaGetErrorString(e));
@@ -706,6 +786,32 @@ rr_status rr_output(rr_solver *s, unsigned what, const char *dir) {
     return RR_OK;
 }
 
+rr_status rr_get_force(rr_solver *s, double *out, int where) {
+    if (!s || !out) return fail(RR_ERR_INVALID, "NULL argument");
+    if (!s->ready) return fail(RR_ERR_STATE, "rr_get_force before rr_init_state / rr_load");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    const size_t n = s->g.n;
+    const double *ff = readout_field(s);
+    if (!ff && s->ffield && s->istep == 0 && s->p.trip_steps > 1) ff = rr::trip_slot(s, 1); // before step 1
+    if (ff) {
+        const cudaMemcpyKind kind = where == RR_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        for (int c = 0; c < 3; c++)
+            RR_CK(cudaMemcpyAsync(out + c * n, ff + (size_t)c * s->g.stride, n * sizeof(double), kind, s->stream));
+        if (where != RR_DEVICE) RR_CK(cudaStreamSynchronize(s->stream));
+        return RR_OK;
+    }
+    if (where == RR_DEVICE) {
+        std::vector<double> h(3 * n);
+        for (int c = 0; c < 3; c++) std::fill(h.begin() + c * n, h.begin() + (c + 1) * n, s->p.force[c]);
+        RR_CK(cudaMemcpyAsync(out, h.data(), 3 * n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        RR_CK(cudaStreamSynchronize(s->stream));
+    } else {
+        RR_CK(cudaStreamSynchronize(s->stream));
+        for (int c = 0; c < 3; c++) std::fill(out + c * n, out + (c + 1) * n, s->p.force[c]);
+    }
+    return RR_OK;
+}
+
 rr_status rr_save(rr_solver *s, const char *dir) { return rr_output(s, RR_OUT_FLOW | RR_OUT_F, dir); }
 
 rr_status rr_load(rr_solver *s, const char *dir, long long istep) {
@@ -728,10 +834,7 @@ rr_status rr_load(rr_solver *s, const char *dir, long long istep) {
     if (st != RR_OK) return st;
     snprintf(name, sizeof name, "/f%09lld.dat", istep);
     if ((st = rd(std::string(dir) + name, f.data(), nf)) != RR_OK) return st;
-    if ((st = rr_init_state(s, f.data(), m.data(), m.data() + n, m.data() + 2 * n, m.data() + 3 * n, RR_HOST)) != RR_OK)
-        return st;
-    s->istep = istep;
-    return RR_OK;
+    return init_state_at(s, f.data(), m.data(), m.data() + n, m.data() + 2 * n, m.data() + 3 * n, RR_HOST, istep);
 }
 
 } // extern "C"

@@ -194,4 +194,54 @@ cudaError_t launch_accumulate(int m, const double *prof, double *acc, cudaStream
     return cudaGetLastError();
 }
 
+// The channel program's start-up trip force of step n (forcing_GP,
+// macrovar.cu:76-115) into fx, fy, fz (3 arrays of stride), or the uniform
+// force (F0, F1, F2) when trip == 0.  amp = (100 beta / LY) sin(2 pi n / 2000),
+// formed on the host; ix / LX is an integer division, as in the reference.
+__global__ void __launch_bounds__(256)
+trip_force_kernel(double *__restrict__ ff, unsigned long long stride, int LX, int LY, int LZ, int trip,
+                  double amp, double phase, double F0, double F1, double F2) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = (uint32_t)LX * (uint32_t)LY * (uint32_t)LZ;
+    if (idx >= n) return;
+    const int ix = (int)(idx % (uint32_t)LX), iy = (int)((idx / (uint32_t)LX) % (uint32_t)LY),
+              iz = (int)(idx / ((uint32_t)LX * (uint32_t)LY));
+    double x = F0, y = F1, z = F2;
+    if (trip) {
+        const double pi2 = 2.0 * 3.14159265358979323846;
+        const double LYq = LY / 4;
+        const int h0 = 2;
+        const double beta9 = 3.0, gamma9 = 2.0;
+        y = 0.0;
+        z = 0.0;
+        if (iy > h0 && iy < LYq + h0) {
+            x = F0 * (1.0 - amp * LX / beta9 * sin(pi2 * (iy - h0) / LYq) * sin(beta9 * pi2 * ix / LX) *
+                                cos(gamma9 * pi2 * iz / LZ));
+            y = F0 * amp * 0.5 * LYq * (1 - cos(pi2 * (iy - h0) / LYq)) * cos(beta9 * pi2 * ix / LX) *
+                cos(gamma9 * pi2 * iz / LZ);
+            z = F0 * amp * 0.5 * LZ / gamma9 * sin(pi2 * (iy - h0) / LYq) * cos(beta9 * pi2 * ix / LX) *
+                sin(gamma9 * pi2 * iz / LZ);
+        } else if (iy > 0.75 * LY - h0 && iy < LY - h0) {
+            const double ph = (double)(ix / LX) + phase;
+            x = F0 * (1.0 + amp * LX / beta9 * sin(pi2 * (-LY + iy + h0 + LYq) / LYq) * sin(beta9 * pi2 * ph) *
+                                cos(gamma9 * pi2 * iz / LZ));
+            y = -F0 * amp * 0.5 * LYq * (1 - cos(pi2 * (-LY + iy + h0 + LYq) / LYq)) * cos(beta9 * pi2 * ph) *
+                cos(gamma9 * pi2 * iz / LZ);
+            z = -F0 * amp * 0.5 * LZ / gamma9 * sin(pi2 * (-LY + iy + h0 + LYq) / LYq) * cos(beta9 * pi2 * ph) *
+                sin(gamma9 * pi2 * iz / LZ);
+        }
+    }
+    ff[idx] = x;
+    ff[stride + idx] = y;
+    ff[2 * stride + idx] = z;
+}
+
+cudaError_t launch_trip_force(double *ff, unsigned long long stride, int LX, int LY, int LZ, int trip, double amp,
+                              double phase, const double F[3], cudaStream_t st) {
+    const unsigned long long n = (unsigned long long)LX * LY * LZ;
+    trip_force_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(ff, stride, LX, LY, LZ, trip, amp, phase, F[0],
+                                                                    F[1], F[2]);
+    return cudaGetLastError();
+}
+
 } // namespace rr

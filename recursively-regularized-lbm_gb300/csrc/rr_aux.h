@@ -24,4 +24,9 @@ cudaError_t launch_profile(const Geom &g, double ystar, const double *ux, const 
 
 cudaError_t launch_accumulate(int m, const double *prof, double *acc, cudaStream_t st);
 
+// the trip force of one step (or the uniform force when trip == 0) into ff
+// (3 arrays of stride); amp = (100 beta / LY) sin(2 pi n / 2000)
+cudaError_t launch_trip_force(double *ff, unsigned long long stride, int LX, int LY, int LZ, int trip, double amp,
+                              double phase, const double F[3], cudaStream_t st);
+
 } // namespace rr

@@ -410,6 +410,9 @@ rr_status rr_batch_add(rr_batch *b, rr_solver *s) {
     if (!b || !s) return rr_internal_error(RR_ERR_INVALID, "NULL argument");
     if (s->batch) return rr_internal_error(RR_ERR_STATE, "the solver is already a member of a batch");
     if (!s->ready) return rr_internal_error(RR_ERR_STATE, "the solver has no state (rr_init_state / rr_load)");
+    if (rr::trip_phase(s, s->istep))
+        return rr_internal_error(RR_ERR_STATE, "the solver is in its trip-forcing phase (until step %d)",
+                                 s->p.trip_steps);
     if (s->p.device != b->device)
         return rr_internal_error(RR_ERR_INVALID, "solver on device %d, batch on device %d", s->p.device, b->device);
     BK(cudaSetDevice(b->device));

@@ -32,9 +32,11 @@ struct Ops {
     // one fused time step over the whole grid in one launch (needs nx >= 3);
     // edges: the x-end nodes of rows on a y/z wall face
     // rows_group: rows per work-item group (a multiple of 32)
+    // ffp, ffc: per-node force fields of the streaming half and of the
+    // collision (3 arrays of g.stride each; NULL: the uniform F; D3Q27 only)
     cudaError_t (*tile)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                         const double F[3], int *status, const uint32_t *edges, uint32_t nedges,
-                        int rows_group, cudaStream_t st);
+                        int rows_group, const double *ffp, const double *ffc, cudaStream_t st);
     // the staged step (needs nx * element size a multiple of 16): rows on a
     // y/z face (frows) in one launch, the interior rows in blocks of R rows
     // through an NS-stage shared-memory pipeline of bulk copies
@@ -64,16 +66,16 @@ struct Ops {
     // (3 arrays of g.stride in the compute type), then tau_t + collision
     cudaError_t (*les2)(int q, bool force, const void *fin, void *fout, const Geom &g, double tau, double cw,
                         const double F[3], int *status, const uint32_t *edges, uint32_t nedges, int rows_group,
-                        void *ubuf, cudaStream_t st);
+                        void *ubuf, const double *ffp, const double *ffc, cudaStream_t st);
     // post-stream populations / macroscopic fields from the post-collision buffer
     cudaError_t (*readout)(int q, bool force, const void *fin, const Geom &g, const double F[3],
                            double *fo, unsigned long long fo_stride, const int *pos, double *rho,
-                           double *ux, double *uy, double *uz, cudaStream_t st);
+                           double *ux, double *uy, double *uz, const double *ff, cudaStream_t st);
     // state upload + first collision with given macros
     cudaError_t (*upload)(int q, bool force, void *fout, const Geom &g, double tau,
                           const double F[3], const double *fi, unsigned long long fi_stride,
                           const int *pos, const double *rho, const double *ux, const double *uy,
-                          const double *uz, const double *taut, cudaStream_t st);
+                          const double *uz, const double *taut, const double *ff, cudaStream_t st);
 };
 
 const Ops &ops_f64();

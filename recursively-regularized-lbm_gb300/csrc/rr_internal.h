@@ -12,6 +12,35 @@
 #include "rr_dispatch.h"
 #include "rr_kernels.cuh"
 
+// The C library's rand() sequence after srand(seed) (the channel program's
+// trip phases come from it), kept per solver: the additive-feedback generator
+// r_i = r_{i-3} + r_{i-31} (mod 2^32), output r_i >> 1, seeded by
+// r_0 = seed, r_i = 16807 r_{i-1} mod (2^31 - 1) for i < 31, r_i = r_{i-31}
+// for 31 <= i < 34, the first 310 outputs discarded.
+struct TripRand {
+    int32_t r[34] = {};
+    int k = 0;
+    void seed(unsigned s0) {
+        int32_t t[344];
+        t[0] = (int32_t)s0;
+        for (int i = 1; i < 31; i++) {
+            long long w = (16807LL * (long long)t[i - 1]) % 2147483647LL;
+            if (w < 0) w += 2147483647LL;
+            t[i] = (int32_t)w;
+        }
+        for (int i = 31; i < 34; i++) t[i] = t[i - 31];
+        for (int i = 34; i < 344; i++) t[i] = (int32_t)((uint32_t)t[i - 31] + (uint32_t)t[i - 3]);
+        for (int i = 0; i < 34; i++) r[i] = t[310 + i];
+        k = 0;
+    }
+    int next() {
+        const int32_t v = (int32_t)((uint32_t)r[(k + 3) % 34] + (uint32_t)r[(k + 31) % 34]);
+        r[k] = v;
+        k = (k + 1) % 34;
+        return (int)((uint32_t)v >> 1);
+    }
+};
+
 struct rr_solver {
     rr_params p;
     const rr::Ops *ops = nullptr;
@@ -45,6 +74,9 @@ struct rr_solver {
     uint32_t nfrows = 0;
     cudaStream_t side = nullptr;     // staged step: the face-row launch, beside the interior one
     cudaEvent_t fork = nullptr, join = nullptr;
+    double *ffield = nullptr;        // trip forcing: the force fields of two steps (2 x 3 arrays of g.stride)
+    TripRand trip_rng;
+    double trip_phase = 0.0;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -61,8 +93,18 @@ inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3
 inline bool staged_ok(const rr_params &p, size_t elem) {
     return !p.use_les && p.lx >= 3 && p.ly >= 3 && p.lz >= 3 && ((size_t)p.lx * elem) % 16 == 0;
 }
-// one step of s from fin to fout on stream st (state bookkeeping is the caller's)
-rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st);
+// one step of s from fin to fout on stream st (state bookkeeping is the
+// caller's); i: the steps done before it (the trip forcing's step number), -1
+// outside the trip phase
+rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st, long long i = -1);
+// the force-field slot of step n (trip forcing)
+double *trip_slot(rr_solver *s, long long n);
+// the force of step n into its slot (redrawing the trip phase when due)
+rr_status trip_prepare(rr_solver *s, long long n, cudaStream_t st);
+// the solver is in its trip-forcing phase for the launch after i steps
+inline bool trip_phase(const rr_solver *s, long long i) {
+    return s->ffield && i >= 0 && i + 1 < s->p.trip_steps;
+}
 // drop the solver's captured step graph (launch shapes or buffers changed)
 void drop_graph(rr_solver *s);
 // tuned launch shapes of a size class, when the autotuner has seen it

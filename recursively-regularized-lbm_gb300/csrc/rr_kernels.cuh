@@ -283,6 +283,10 @@ struct TileArgs {
     int *status;
     typename CType<S>::T *u; // WALE passes: velocity field, 3 arrays of g.stride
     double tau, cw;          // WALE collide pass: molecular tau, C_w
+    // per-node force fields (3 arrays of g.stride each; FIELD instantiations):
+    // ffp for the streaming half of the step (walls, moments), ffc for the
+    // collision
+    const double *ffp, *ffc;
 };
 
 // populations entering the domain through face F (0..5 = x-lo .. z-hi)
@@ -421,7 +425,7 @@ __device__ __forceinline__ T les_taut(const T *__restrict__ u, const Geom &g, in
 // DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
 // applies the walls and writes the velocity field; MODE 2 streams again,
 // takes tau_t from the 7-point stencil of that field and collides.
-template <class LT, typename S, bool FORCE, int MODE = 0, class A>
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
     using T = typename CType<S>::T;
     if (item >= a.nitems) return;
@@ -474,7 +478,20 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
         fast = false;
     }
     const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
-    const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    // the force of the streaming half (walls, moments) and of the collision
+    T Fx, Fy, Fz, Cx, Cy, Cz;
+    if constexpr (FIELD) {
+        Fx = T(a.ffp[idx]);
+        Fy = T(a.ffp[g.stride + idx]);
+        Fz = T(a.ffp[2 * g.stride + idx]);
+        Cx = T(a.ffc[idx]);
+        Cy = T(a.ffc[g.stride + idx]);
+        Cz = T(a.ffc[2 * g.stride + idx]);
+    } else {
+        Fx = Cx = T(a.F[0]);
+        Fy = Cy = T(a.F[1]);
+        Fz = Cz = T(a.F[2]);
+    }
     T d[LT::Q];
     if (fast) {
         static_for<LT::Q>([&](auto ic) {
@@ -537,7 +554,7 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
     T om1 = T(a.om1);
     if constexpr (MODE == 2) om1 = T(1) - T(1) / (T(a.tau) + les_taut<T>(a.u, g, x, y, z, idx, T(a.cw)));
-    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Fx, Fy, Fz);
+    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Cx, Cy, Cz);
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (g.sround) {
             store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
@@ -550,10 +567,11 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     });
 }
 
-template <class LT, typename S, bool FORCE, int MODE = 0>
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false>
 __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    tile_item<LT, S, FORCE, MODE>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+    tile_item<LT, S, FORCE, MODE, FIELD>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
+
 
 // Many domains in one persistent launch.  The CTAs of every domain's tile
 // step (blockDim / 32 items each) are numbered consecutively, domain after
@@ -615,10 +633,15 @@ __global__ void __launch_bounds__(256)
 readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double Fz_,
                double *__restrict__ fo, unsigned long long fo_stride, const int *__restrict__ pos,
                double *__restrict__ rho, double *__restrict__ ux_o, double *__restrict__ uy_o,
-               double *__restrict__ uz_o) {
+               double *__restrict__ uz_o, const double *__restrict__ ff) {
     using T = typename CType<S>::T;
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= g.n) return;
+    if (ff) { // a per-node force field: 3 arrays of g.stride
+        Fx_ = ff[idx];
+        Fy_ = ff[g.stride + idx];
+        Fz_ = ff[2 * g.stride + idx];
+    }
     int x, y, z;
     node_xyz(idx, g.nx, g.ny, x, y, z);
     T d[LT::Q];
@@ -662,10 +685,15 @@ upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, 
               const double *__restrict__ fi, unsigned long long fi_stride, const int *__restrict__ pos,
               const double *__restrict__ rho, const double *__restrict__ ux,
               const double *__restrict__ uy, const double *__restrict__ uz,
-              const double *__restrict__ taut) {
+              const double *__restrict__ taut, const double *__restrict__ ff) {
     using T = typename CType<S>::T;
     const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= g.n) return;
+    if (ff) { // a per-node force field: 3 arrays of g.stride
+        Fx_ = ff[idx];
+        Fy_ = ff[g.stride + idx];
+        Fz_ = ff[2 * g.stride + idx];
+    }
     T d[LT::Q];
     if (fi) {
         // internal population i is input population pos[i]

@@ -40,7 +40,7 @@ class Params(ctypes.Structure):
                 ("cw", ctypes.c_double), ("force", ctypes.c_double * 3),
                 ("face", ctypes.c_int * 6), ("uwall", (ctypes.c_double * 3) * 6),
                 ("storage", ctypes.c_int), ("order", ctypes.c_int), ("device", ctypes.c_int),
-                ("ustar", ctypes.c_double), ("ystar", ctypes.c_double), ("rounding", ctypes.c_int)]
+                ("ustar", ctypes.c_double), ("ystar", ctypes.c_double), ("rounding", ctypes.c_int), ("trip_steps", ctypes.c_int)]
 
     @property
     def n(self):
@@ -80,6 +80,7 @@ def lib():
             "rr_get_accum": ([vp, dp, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
             "rr_output": ([vp, ctypes.c_uint, ctypes.c_char_p], ctypes.c_int),
             "rr_save": ([vp, ctypes.c_char_p], ctypes.c_int),
+            "rr_get_force": ([vp, vp, ctypes.c_int], ctypes.c_int),
             "rr_load": ([vp, ctypes.c_char_p, ctypes.c_longlong], ctypes.c_int),
             "rr_device_bytes": ([vp], ctypes.c_size_t),
             "rr_bytes_for": ([P], ctypes.c_size_t),
@@ -218,6 +219,12 @@ class Solver:
         ptrs = [_ptr(a) for a in (rho, ux, uy, uz, taut)]
         where = ptrs[0][1]
         _check(lib().rr_macro(self._h, *[p_ for p_, _ in ptrs], where))
+
+    def get_force(self):
+        """the body force (fx, fy, fz fields) of the step the readouts show"""
+        out = np.empty((3,) + self.p.shape)
+        _check(lib().rr_get_force(self._h, out.ctypes.data, HOST))
+        return out
 
     def get_f(self):
         f = np.empty((self.p.q,) + self.p.shape)

@@ -248,3 +248,50 @@ def test_laminar_channel_golden():
             print(f"\nlaminar step {step}: GPU max |uy - ref| / max uy = {err:.2e}")
             assert err < 1e-8, (step, err)
             assert np.abs(m["uy"] - o.uy).max() / np.abs(ref).max() < 1e-11
+
+
+@pytest.mark.parametrize("les", [False, True])
+def test_trip_forcing(les):
+    """The channel program's start-up trip forcing (forcing_GP with the rand()
+    phase) against the oracle, which is pinned bit for bit to the reference's
+    kernels.  The flow to step 400 (later steps of this small forced channel
+    amplify roundoff by about 10 per 300 steps, trip or not); the force field
+    itself, which the solver reads out, across the phase draws at steps 2000
+    and 4000 and the switch to the uniform force at step 4050."""
+    import ctypes
+    from oracle import oracle as O
+
+    p, st = presets.channel(nx=16, ny=12, nz=8, les=les, variant="reference")
+    p.trip_steps = 4050
+    o = oracle_for(p)
+    load_state(o, st)
+    o.enable_trip(4050)
+    ref_rand = O.Trip()
+    O.lib().orc_srand(ctypes.byref(ref_rand), 12345)
+    phase = 0.0
+    want = np.empty((3,) + o.shape)
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
+        done = 0
+        for n in (1, 100, 400, 1999, 2000, 2001, 4000, 4049, 4050, 4051):
+            s.step(n - done)
+            if n <= 400:
+                o.run(n - done)
+                m = s.macro()
+                scale = st["ustar"] * 20
+                for k, ref in (("ux", o.ux), ("uy", o.uy), ("uz", o.uz)):
+                    err = np.abs(m[k] - ref).max() / scale
+                    assert err < 1e-12, (n, k, err)
+                assert np.abs(m["rho"] - o.rho).max() < 1e-13, n
+            # the oracle's field of step n (phases drawn at steps 2000, 4000)
+            for k in range(done + 1, n + 1):
+                if k % 2000 == 0 and k < 4050:
+                    phase = O.lib().orc_rand(ctypes.byref(ref_rand)) / 2147483647.0
+            done = n
+            if n < 4050:
+                P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                O.lib().orc_trip_force(ctypes.byref(o.P), n, phase, P(want[0]), P(want[1]), P(want[2]))
+            else:
+                want[0], want[1], want[2] = p.force[0], 0.0, 0.0
+            got = s.get_force()
+            assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max(), n
