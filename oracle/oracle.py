@@ -42,7 +42,7 @@ class Params(ctypes.Structure):
                 ("lat", Lattice), ("tau", ctypes.c_double), ("force", ctypes.c_double * 3),
                 ("les", ctypes.c_int), ("cw", ctypes.c_double), ("face", ctypes.c_int * 6),
                 ("uwall", (ctypes.c_double * 3) * 6), ("tg_real4", ctypes.c_int),
-                ("ffield", ctypes.POINTER(ctypes.c_double))]
+                ("ffield", ctypes.POINTER(ctypes.c_double)), ("bgk", ctypes.c_int)]
 
 
 class Trip(ctypes.Structure):
@@ -110,7 +110,7 @@ class Sim:
     """A grid in the reference's own state form (post-stream f + macros)."""
 
     def __init__(self, nx, ny, nz, q=27, order=ORDER_CUDA, cs_mode=CS_SQRT_RT, tau=0.6,
-                 force=(0.0, 0.0, 0.0), les=False, cw=0.5, faces=(0,) * 6, uwall=None):
+                 force=(0.0, 0.0, 0.0), les=False, cw=0.5, faces=(0,) * 6, uwall=None, bgk=False):
         P = Params()
         P.nx, P.ny, P.nz = nx, ny, nz
         P.lat = lattice(q, order, cs_mode)
@@ -118,6 +118,7 @@ class Sim:
         for i in range(3):
             P.force[i] = force[i]
         P.les = int(bool(les))
+        P.bgk = int(bool(bgk))
         P.cw = cw
         for i in range(6):
             P.face[i] = faces[i]

@@ -44,10 +44,44 @@ EOP
         "$REF/BC.cu" "$REF/LES.cu" "$HERE/ref_driver.cpp" -o "$OUT/$NAME"
     echo "built $OUT/$NAME"
 }
+# the BGK channel program (BGK/): its kernels and its globals, one grid
+build_bgk() {
+    LX=$1; LY=$2; LZ=$3
+    BREF=${RR_REFERENCE_DIR:-/root/reference}/BGK
+    [ -f "$BREF/collision.cu" ] || return 0
+    NAME="libref_bgk_${LX}x${LY}x${LZ}.so"
+    P="$OUT/params_bgk_${LX}x${LY}x${LZ}.h"
+    cat > "$P" <<EOP
+#ifndef PARAMETERS_H
+#define PARAMETERS_H
+#define CONTINUE_STEP 0
+#define LX $LX
+#define LY $LY
+#define LZ $LZ
+#define LXYZ (LX * LY * LZ)
+#define NPOP 27
+#define NEND 10
+#define NDIAG 10
+#define NFLOWOUT 5000
+#define NNUOUT 10
+#define GRAVITY 1.0
+#define BETA (0.1 / (LY * 5.0))
+#define BLOCK_X 8
+#define BLOCK_Y 4
+#define BLOCK_Z 4
+#endif
+EOP
+    $CXX -O2 -fPIC -fopenmp -ffp-contract=off -std=c++14 -w -shared \
+        -I "$HERE/ref_shim" -I "$BREF" -include "$P" -x c++ \
+        "$BREF/globals.cu" "$BREF/collision.cu" "$BREF/streaming.cu" "$BREF/macrovar.cu" \
+        "$HERE/ref_driver_bgk.cpp" -o "$OUT/$NAME"
+    echo "built $OUT/$NAME"
+}
 if [ $# -ge 4 ]; then
     while [ $# -ge 4 ]; do build_one "$1" "$2" "$3" "$4"; shift 4; done
 else
     # grids used by the parity tests
     build_one 16 12 8 0
     build_one 16 12 8 1
+    build_bgk 16 12 8
 fi

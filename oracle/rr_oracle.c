@@ -438,7 +438,42 @@ void orc_moments_all(const orc_params *P, const double *f, double *rho, double *
         for (int ip = 0; ip < L->q; ip++) fl[ip] = f[ip * N + idx];
         double Fn[3];
         node_force(P, N, idx, Fn);
-        orc_moments_node(L, Fn, fl, &rho[idx], &ux[idx], &uy[idx], &uz[idx]);
+        if (P->bgk) {
+            /* BGK/macrovar.cu:16-30: rho = sum f, u = sum c f + F/2 */
+            double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+            for (int ip = 0; ip < L->q; ip++) {
+                r += fl[ip];
+                jx += L->cx[ip] * fl[ip];
+                jy += L->cy[ip] * fl[ip];
+                jz += L->cz[ip] * fl[ip];
+            }
+            rho[idx] = r;
+            ux[idx] = jx + 0.5 * Fn[0];
+            uy[idx] = jy + 0.5 * Fn[1];
+            uz[idx] = jz + 0.5 * Fn[2];
+        } else {
+            orc_moments_node(L, Fn, fl, &rho[idx], &ux[idx], &uy[idx], &uz[idx]);
+        }
+    }
+}
+
+/* BGK/collision.cu:11-33: feq = w (rho + eu + (eu^2 - uv) / 2) with
+ * eu = c.u / RT, uv = u.u / RT; f += -(f - feq) / tau + (1 - 0.5 / tau)
+ * (c.F - u.F) / RT w (1 + eu + (eu^2 - uv) / 2) */
+void orc_bgk_node(const orc_lattice *L, double tau, const double F[3], double rho9, double u9, double v9,
+                  double w9, double *f) {
+    const double fx9 = F[0], fy9 = F[1], fz9 = F[2];
+    const double G3 = u9 * fx9 + v9 * fy9 + w9 * fz9;
+    for (int ip = 0; ip < L->q; ip++) {
+        const double RT = 1.0 / 3.0;
+        const double eu = (L->cx[ip] * u9 + L->cy[ip] * v9 + L->cz[ip] * w9) / RT;
+        const double uv = (u9 * u9 + v9 * v9 + w9 * w9) / RT;
+        const double feq = L->w[ip] * (rho9 + eu + 0.5 * (eu * eu - uv));
+        const double G1 = L->cx[ip] * fx9 + L->cy[ip] * fy9 + L->cz[ip] * fz9;
+        double fchange = -(f[ip] - feq) / tau;
+        const double feq_rho0 = L->w[ip] * (1.0 + eu + 0.5 * (eu * eu - uv));
+        fchange += (1.0 - 0.5 / tau) * (G1 - G3) / RT * feq_rho0;
+        f[ip] += fchange;
     }
 }
 
@@ -454,7 +489,11 @@ void orc_collide_all(const orc_params *P, double *f, const double *rho, const do
         for (int ip = 0; ip < L->q; ip++) fl[ip] = f[ip * N + idx];
         /* collision.cu:27-31 */
         double tau_eff = P->les ? P->tau + taut[idx] : P->tau;
-        if (P->tg_real4)
+        if (P->bgk) {
+            double Fn[3];
+            node_force(P, N, idx, Fn);
+            orc_bgk_node(L, P->tau, Fn, rho[idx], ux[idx], uy[idx], uz[idx], fl);
+        } else if (P->tg_real4)
             collide_node_tg4(L, &T, tau_eff, rho[idx], ux[idx], uy[idx], uz[idx], fl);
         else {
             double Fn[3];

@@ -69,6 +69,10 @@ typedef struct {
     /* per-node body force (fx, fy, fz: three arrays of nx ny nz), or NULL
      * for the uniform force above */
     const double *ffield;
+    /* BGK single-relaxation-time collision of the BGK program instead of the
+     * RR one (BGK/collision.cu:3-34), with its incompressible velocity
+     * u = sum c f + F/2 (BGK/macrovar.cu:4-31) */
+    int bgk;
 } orc_params;
 
 /* State in the reference's own form: populations after streaming and wall
@@ -85,6 +89,8 @@ double orc_feq(const orc_lattice *L, int ip, double rho9, double u9, double v9, 
 
 void orc_collide_node(const orc_lattice *L, double tau_eff, const double F[3], double rho9,
                       double u9, double v9, double w9, double *f);
+void orc_bgk_node(const orc_lattice *L, double tau, const double F[3], double rho9, double u9, double v9,
+                  double w9, double *f);
 
 void orc_regularize_node(const orc_lattice *L, const double F[3], double *f,
                          const int *entering);

@@ -181,3 +181,34 @@ def test_trip_forcing_matches_reference_live(les):
     assert np.array_equal(s.f, f)
     for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
         assert np.array_equal(getattr(s, k), a), k
+
+
+def test_bgk_matches_reference_live():
+    """The oracle's BGK collision (BGK/collision.cu) and incompressible
+    moments (BGK/macrovar.cu) with half-way bounce-back at y walls against the
+    BGK program's own kernels built for the host, bit for bit."""
+    path = os.path.join(ROOT, "oracle", "_ref", "libref_bgk_16x12x8.so")
+    if not os.path.exists(path):
+        pytest.skip("reference kernels not built here (oracle/ref_build.sh needs the reference sources)")
+    R = ctypes.CDLL(path)
+    for n in ("bgk_tau", "bgk_force_in_x"):
+        getattr(R, n).restype = ctypes.c_double
+    R.bgk_init_constants()
+    tau, fx0 = R.bgk_tau(), R.bgk_force_in_x()
+    s = O.Sim(16, 12, 8, q=27, order=O.ORDER_CUDA, cs_mode=O.CS_SQRT_RT, tau=tau, force=(fx0, 0.0, 0.0),
+              faces=(0, 0, 2, 2, 0, 0), bgk=True)
+    rng = np.random.default_rng(3)
+    s.ux[...] = 0.02 * rng.standard_normal(s.shape)
+    s.uy[...] = 0.01 * rng.standard_normal(s.shape)
+    s.uz[...] = 0.01 * rng.standard_normal(s.shape)
+    s.rho[...] = 1.0 + 1e-3 * rng.standard_normal(s.shape)
+    s.init_equilibrium2()
+    s.f *= 1.0 + 1e-3 * rng.standard_normal(s.f.shape)
+    f, rho, ux, uy, uz = (a.copy() for a in (s.f, s.rho, s.ux, s.uy, s.uz))
+    ft, fx, fy, fz = (np.zeros_like(a) for a in (f, rho, rho, rho))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    R.bgk_run(25, P(f), P(ft), P(rho), P(ux), P(uy), P(uz), P(fx), P(fy), P(fz))
+    s.run(25)
+    assert np.array_equal(s.f, f)
+    for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
+        assert np.array_equal(getattr(s, k), a), k
