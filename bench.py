@@ -53,6 +53,7 @@ WORKLOADS = {
     "channel_les_f16": dict(kind="channel", storage="f16"),
     "tg100_f64": dict(kind="tg", storage="f64"),
     "tg128_f16": dict(kind="tg128", storage="f16"),
+    "tg128_bgk_f16": dict(kind="tg128", storage="f16", bgk=True),
 }
 BYTES_PER_POP = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}
 DTYPE = {"f64": "f64", "f32": "f32", "f16": "f16-store/f32-compute", "bf16": "bf16-store/f32-compute"}
@@ -66,7 +67,12 @@ def make(wl):
     if w["kind"] == "channel":
         return presets.channel(storage=w["storage"], les=True, variant="config")
     if w["kind"] == "tg128":
-        return presets.taylor_green(L=128, nz=128, tau=0.6, Ma=0.05, storage=w["storage"])
+        p, st = presets.taylor_green(L=128, nz=128, tau=0.6, Ma=0.05, storage=w["storage"])
+        if w.get("bgk"):
+            import rrlbm
+            p.collision = rrlbm.COLL_BGK
+            st["f"] = None  # the BGK run starts from the second-order equilibrium of the fields
+        return p, st
     return presets.taylor_green(L=100, nz=4, tau=0.6, Ma=0.01, storage=w["storage"])
 
 
@@ -79,7 +85,8 @@ def describe(wl, p, storage):
         return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 RR + WALE (C_w=0.5), Re_tau=180, walls y, periodic x/z, "
                 f"body force, {storage} storage")
     ma = 0.05 if kind == "tg128" else 0.01
-    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Ma={ma}, tau=0.6, periodic, {storage} storage"
+    coll = "BGK" if WORKLOADS[wl].get("bgk") else "RR"
+    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 {coll}, Ma={ma}, tau=0.6, periodic, {storage} storage"
 
 
 def peaks():

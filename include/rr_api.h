@@ -97,7 +97,15 @@ typedef struct rr_params {
      * force.  0 (default): off; the reference's value is 50000.  D3Q27 and
      * lx >= 3 only; steps in the trip phase run without CUDA graphs. */
     int trip_steps;
+    /* rr_collision: the RR collision (default), or the BGK program's
+     * single-relaxation-time collision with its incompressible velocity
+     * u = sum c f + F/2 (BGK/collision.cu:3-34, BGK/macrovar.cu:4-31); BGK
+     * needs D3Q27, DNS, lx >= 3, bounce-back walls without the regularized
+     * closure (RR_FACE_WALL_BB) and no trip forcing */
+    int collision;
 } rr_params;
+
+typedef enum { RR_COLL_RR = 0, RR_COLL_BGK = 1 } rr_collision;
 
 typedef struct rr_solver rr_solver;
 

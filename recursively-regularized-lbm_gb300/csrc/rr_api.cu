@@ -99,6 +99,16 @@ rr_status validate(const rr_params *p) {
     if (p->trip_steps < 0) return fail(RR_ERR_INVALID, "trip_steps = %d", p->trip_steps);
     if (p->trip_steps > 0 && (p->q != 27 || p->lx < 3))
         return fail(RR_ERR_UNSUPPORTED, "trip forcing needs D3Q27 and lx >= 3");
+    if (p->collision != RR_COLL_RR && p->collision != RR_COLL_BGK)
+        return fail(RR_ERR_INVALID, "collision = %d unknown", p->collision);
+    if (p->collision == RR_COLL_BGK) {
+        if (p->q != 27 || p->use_les || p->lx < 3 || p->trip_steps > 0)
+            return fail(RR_ERR_UNSUPPORTED, "the BGK collision needs D3Q27, DNS, lx >= 3 and no trip forcing");
+        for (int f = 0; f < 6; f++)
+            if (p->face[f] == RR_FACE_WALL)
+                return fail(RR_ERR_UNSUPPORTED, "the BGK collision takes bounce-back walls (RR_FACE_WALL_BB), "
+                                                "not the regularized closure");
+    }
     return RR_OK;
 }
 
@@ -252,7 +262,7 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         else
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
                                    s->tile, st));
-    } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list && !ffp) {
+    } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list && !ffp && !s->g.bgk) {
         RR_CK(s->ops->staged(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
                              s->frow_list, s->nfrows, s->stage_rows, s->stages, st, s->side, s->fork, s->join));
     } else if (s->p.lx >= 3) {
@@ -461,6 +471,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         s->bytes += lb;
     }
     g.sround = (p->rounding == RR_ROUND_STOCHASTIC) ? 1 : 0;
+    g.bgk = p->collision == RR_COLL_BGK ? 1 : 0;
     if (const size_t ub = les_ubuf_bytes(*p)) {
         if (cudaMalloc(&s->ubuf, ub) != cudaSuccess) {
             cudaGetLastError();

@@ -87,11 +87,12 @@ namespace rr {
 
 bool has_force(const rr_params &p);
 // the step kind of a solver: the tile step (one launch, batchable) or not
-inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3; }
+inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3 && !s->g.bgk; }
 // the staged step applies: DNS, at least 3 nodes on every axis, rows a
 // multiple of 16 bytes (bulk copies)
 inline bool staged_ok(const rr_params &p, size_t elem) {
-    return !p.use_les && p.lx >= 3 && p.ly >= 3 && p.lz >= 3 && ((size_t)p.lx * elem) % 16 == 0;
+    return !p.use_les && p.collision == RR_COLL_RR && p.lx >= 3 && p.ly >= 3 && p.lz >= 3 &&
+           ((size_t)p.lx * elem) % 16 == 0;
 }
 // one step of s from fin to fout on stream st (state bookkeeping is the
 // caller's); i: the steps done before it (the trip forcing's step number), -1

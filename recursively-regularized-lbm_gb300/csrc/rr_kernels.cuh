@@ -39,6 +39,7 @@ struct Geom {
     double uw[6][3];     // wall velocity of each face
     uint32_t wallmask;   // bit f: face f is a wall
     int sround;          // FP16/BF16 storage: stochastic (1) or nearest (0) rounding
+    int bgk;             // BGK collision with the incompressible velocity (else RR)
 };
 
 template <typename S> struct CType { using T = float; };
@@ -420,12 +421,33 @@ __device__ __forceinline__ T les_taut(const T *__restrict__ u, const Geom &g, in
     return wale_tau_t(gr, cw);
 }
 
+// BGK single-relaxation-time collision of the BGK program (BGK/collision.cu:
+// 11-33) in deviation form d = f / w - 1: feq / w = rho + p with
+// p = eu + (eu^2 - uv) / 2, eu = 3 c.u, uv = 3 u.u, so
+// d* = d - (d - (drho + p)) / tau + (1 - 1 / (2 tau)) 3 (c.F - u.F) (1 + p)
+template <class LT, typename T, bool FORCE>
+__host__ __device__ __forceinline__ void collide_bgk(T (&d)[LT::Q], T drho, T ux, T uy, T uz, T inv_tau, T Fx,
+                                                     T Fy, T Fz) {
+    const T uv = T(3) * (ux * ux + uy * uy + uz * uz);
+    const T kf = T(1) - T(0.5) * inv_tau;
+    const T uF = ux * Fx + uy * Fy + uz * Fz;
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        constexpr int cx = LT::cx(i), cy = LT::cy(i), cz = LT::cz(i);
+        const T eu = T(3) * (T(cx) * ux + T(cy) * uy + T(cz) * uz);
+        const T p = eu + T(0.5) * (eu * eu - uv);
+        T v = d[i] - (d[i] - (drho + p)) * inv_tau;
+        if constexpr (FORCE) v += kf * T(3) * (T(cx) * Fx + T(cy) * Fy + T(cz) * Fz - uF) * (T(1) + p);
+        d[i] = v;
+    });
+}
+
 // one work item (one warp) of the tile step; A is TileArgs wherever it lives
 // (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
 // DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
 // applies the walls and writes the velocity field; MODE 2 streams again,
 // takes tau_t from the 7-point stencil of that field and collides.
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, class A>
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
     using T = typename CType<S>::T;
     if (item >= a.nitems) return;
@@ -544,7 +566,14 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     }
     Mom<T> m = moments<LT>(d);
     T ux, uy, uz;
-    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if constexpr (BGK) {
+        // BGK/macrovar.cu:27-29: u = sum c f + F/2
+        ux = m.jx + T(0.5) * Fx;
+        uy = m.jy + T(0.5) * Fy;
+        uz = m.jz + T(0.5) * Fz;
+    } else {
+        velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    }
     if constexpr (MODE == 1) {
         a.u[idx] = ux;
         a.u[g.stride + idx] = uy;
@@ -554,7 +583,8 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
     T om1 = T(a.om1);
     if constexpr (MODE == 2) om1 = T(1) - T(1) / (T(a.tau) + les_taut<T>(a.u, g, x, y, z, idx, T(a.cw)));
-    collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Cx, Cy, Cz);
+    if constexpr (BGK) collide_bgk<LT, T, FORCE>(d, m.drho, ux, uy, uz, T(1) - om1, Cx, Cy, Cz);
+    else collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, om1, Cx, Cy, Cz);
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (g.sround) {
             store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
@@ -567,9 +597,9 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     });
 }
 
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false>
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
 __global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    tile_item<LT, S, FORCE, MODE, FIELD>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+    tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
 
 
@@ -669,9 +699,10 @@ readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double
             if constexpr (LT::cz(i) < 0) jz -= fv;
         });
         rho[idx] = r;
-        ux_o[idx] = (jx + 0.5 * Fx_) / r;
-        uy_o[idx] = (jy + 0.5 * Fy_) / r;
-        uz_o[idx] = (jz + 0.5 * Fz_) / r;
+        // BGK: the incompressible velocity, not divided by rho
+        ux_o[idx] = g.bgk ? jx + 0.5 * Fx_ : (jx + 0.5 * Fx_) / r;
+        uy_o[idx] = g.bgk ? jy + 0.5 * Fy_ : (jy + 0.5 * Fy_) / r;
+        uz_o[idx] = g.bgk ? jz + 0.5 * Fz_ : (jz + 0.5 * Fz_) / r;
     }
 }
 
@@ -714,8 +745,12 @@ upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, 
     }
     Mom<T> m = moments<LT>(d);
     const double tau_eff = taut ? tau + taut[idx] : tau;
-    collide<LT, T, FORCE>(d, m, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]),
-                          T(1.0 - 1.0 / tau_eff), T(Fx_), T(Fy_), T(Fz_));
+    if (g.bgk)
+        collide_bgk<LT, T, FORCE>(d, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]), T(1.0 / tau_eff),
+                                  T(Fx_), T(Fy_), T(Fz_));
+    else
+        collide<LT, T, FORCE>(d, m, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]),
+                              T(1.0 - 1.0 / tau_eff), T(Fx_), T(Fy_), T(Fz_));
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
         st_dev<T>(fout + (unsigned long long)i * g.stride + idx, d[i]);

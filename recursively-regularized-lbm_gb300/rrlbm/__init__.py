@@ -18,6 +18,7 @@ LIBPATH = os.path.join(_HERE, "librrlbm.so")
 STORE_F64, STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2, 3
 STORAGE = {"f64": STORE_F64, "f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
 FACE_PERIODIC, FACE_WALL, FACE_WALL_BB = 0, 1, 2
+COLL_RR, COLL_BGK = 0, 1
 ROUND_NEAREST, ROUND_STOCHASTIC = 0, 1
 ORDER_CUDA, ORDER_FORTRAN = 0, 1
 HOST, DEVICE = 0, 1
@@ -40,7 +41,7 @@ class Params(ctypes.Structure):
                 ("cw", ctypes.c_double), ("force", ctypes.c_double * 3),
                 ("face", ctypes.c_int * 6), ("uwall", (ctypes.c_double * 3) * 6),
                 ("storage", ctypes.c_int), ("order", ctypes.c_int), ("device", ctypes.c_int),
-                ("ustar", ctypes.c_double), ("ystar", ctypes.c_double), ("rounding", ctypes.c_int), ("trip_steps", ctypes.c_int)]
+                ("ustar", ctypes.c_double), ("ystar", ctypes.c_double), ("rounding", ctypes.c_int), ("trip_steps", ctypes.c_int), ("collision", ctypes.c_int)]
 
     @property
     def n(self):

@@ -10,7 +10,7 @@ def oracle_for(p, les=None):
     order = O.ORDER_CUDA if p.q == 27 else O.ORDER_FORTRAN
     return O.Sim(p.lx, p.ly, p.lz, q=p.q, order=order, cs_mode=O.CS_SQRT_RT, tau=p.tau,
                  force=tuple(p.force), les=bool(p.use_les if les is None else les), cw=p.cw,
-                 faces=tuple(p.face), uwall=[list(p.uwall[f]) for f in range(6)])
+                 faces=tuple(p.face), uwall=[list(p.uwall[f]) for f in range(6)], bgk=p.collision == 1)
 
 
 def load_state(o, st):

@@ -295,3 +295,27 @@ def test_trip_forcing(les):
                 want[0], want[1], want[2] = p.force[0], 0.0, 0.0
             got = s.get_force()
             assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max(), n
+
+
+@pytest.mark.parametrize("case", ["channel", "tg"])
+def test_bgk_collision(case):
+    """The BGK program's collision (incompressible velocity, bounce-back walls)
+    against the oracle, which is pinned bit for bit to that program's kernels."""
+    if case == "channel":
+        p, st = presets.channel(nx=16, ny=12, nz=8, Re_tau=20, les=False, variant="config", amp=0.2)
+        p.face[2] = p.face[3] = rrlbm.FACE_WALL_BB
+        scale = st["uc"]
+    else:
+        p, st = presets.taylor_green(L=24, nz=6, tau=0.7, Ma=0.08)
+        st["f"] = None
+        scale = st["U0"]
+    p.collision = rrlbm.COLL_BGK
+    _check(_run_pair(p, st, [1, 20, 100]), scale)
+
+
+def test_bgk_rejects_regularized_walls():
+    p, st = presets.cavity(n=8)
+    p.collision = rrlbm.COLL_BGK
+    with pytest.raises(rrlbm.RRError) as e:
+        rrlbm.Solver(p)
+    assert e.value.code == 4
