@@ -50,6 +50,10 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
@@ -92,60 +96,68 @@ __device__ __forceinline__ void stage_block(uint32_t b, const FastDiv &div_ybloc
     rows = min((int)R, ny - 1 - y0);
 }
 
+constexpr int STAGE_CONSUMERS = 256;                  // compute threads (8 warps)
+constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
+
+// Warp-specialised pipeline.  Warp 8 (its lane 0) is the producer: for each
+// of the CTA's blocks it waits until the 8 compute warps have released the
+// stage (empty barrier, one arrive per warp), then issues the block's bulk
+// copies onto the stage's full barrier.  The compute warps wait on the full
+// barrier, compute, and release the stage; no barrier over the whole CTA.
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256, 4) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(stage_smem);
+    uint64_t *full = reinterpret_cast<uint64_t *>(stage_smem);  // [STAGE_MAX]
+    uint64_t *empty = full + STAGE_MAX;                         // [STAGE_MAX]
     S *buf = reinterpret_cast<S *>(stage_smem + 128);
-    __shared__ int s_fail;
     const Geom &g = a.g;
     const int nx = g.nx;
     const uint32_t NS = a.stages;
     const uint32_t R = a.rows;
     if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        for (uint32_t s = 0; s < NS; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], STAGE_CONSUMERS / 32);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_fail = 0;
     }
     __syncthreads();
     // blocks of this CTA: blockIdx.x + k gridDim.x, k = 0 .. mine-1
     const uint32_t mine = blockIdx.x < a.nblocks ? (a.nblocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    // the issuing thread: Q bulk copies of the CTA's k-th block into stage k % NS
-    auto issue = [&](uint32_t k) {
-        int z, y0, rows;
-        stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
-        const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
-        uint64_t *b = &bar[k % NS];
-        S *st = buf + (size_t)(k % NS) * a.stage_elems;
-        mbar_expect_tx(b, (uint32_t)LT::Q * bytes);
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            const size_t src = (size_t)i * g.stride +
-                               ((size_t)(z - LT::cz(i)) * (size_t)g.ny + (size_t)(y0 - LT::cy(i))) * (size_t)nx;
-            bulk_g2s(st + (size_t)i * R * nx, a.fin + src, bytes, b);
-        });
-    };
-    uint32_t issued = 0, kfail = 0;
-    if (threadIdx.x == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (; issued < mine && issued + 1 < NS; issued++) issue(issued);
+    if (threadIdx.x >= STAGE_CONSUMERS) {
+        if (threadIdx.x != STAGE_CONSUMERS) return;
+        // the producer
+        uint32_t k = 0;
+        for (; k < mine; k++) {
+            const uint32_t s = k % NS;
+            if (k >= NS && !mbar_wait(&empty[s], (k / NS - 1) & 1u, STAGE_WAIT_LIMIT)) {
+                atomicOr(a.status, 4);
+                break;
+            }
+            int z, y0, rows;
+            stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
+            const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
+            S *st = buf + (size_t)s * a.stage_elems;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&full[s], (uint32_t)LT::Q * bytes);
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                const size_t src = (size_t)i * g.stride +
+                                   ((size_t)(z - LT::cz(i)) * (size_t)g.ny + (size_t)(y0 - LT::cy(i))) * (size_t)nx;
+                bulk_g2s(st + (size_t)i * R * nx, a.fin + src, bytes, &full[s]);
+            });
+        }
+        // before the CTA may leave, every copy it issued has landed (the last
+        // use of each stage; bounded)
+        for (uint32_t j = (k > NS ? k - NS : 0); j < k; j++)
+            mbar_wait(&full[j % NS], (j / NS) & 1u, STAGE_WAIT_LIMIT);
+        return;
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
     for (uint32_t k = 0; k < mine; k++) {
-        if (threadIdx.x == 0 && issued < mine) {
-            // stage (k + NS - 1) % NS was read in iteration k - 1, closed by its barrier
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(issued);
-            issued++;
-        }
-        const bool ok = mbar_wait(&bar[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                s_fail = 1;
-                kfail = k;
-                atomicOr(a.status, 4);
-            }
+        if (!mbar_wait(&full[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT)) {
+            if ((threadIdx.x & 31u) == 0) atomicOr(a.status, 4);
             break;
         }
         int z, y0, rows;
@@ -157,8 +169,8 @@ __global__ void __launch_bounds__(256, 4) stage_kernel(const __grid_constant__ S
         const int nxi = xwall ? nx - 2 : nx;
         const int nmain = rows * nxi;
         const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
-        const int total = ((nmain + (int)blockDim.x - 1) / (int)blockDim.x) * (int)blockDim.x + nwall;
-        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nwall;
+        for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
             int r, x;
             if (t < nmain) {
                 r = (int)fdiv((uint32_t)t, a.div_nxi);
@@ -225,12 +237,9 @@ __global__ void __launch_bounds__(256, 4) stage_kernel(const __grid_constant__ S
                 st_dev<T>(a.dst[i] + idx, d[i]);
             });
         }
-        __syncthreads(); // stage k % NS is free again
-    }
-    if (s_fail && threadIdx.x == 0) {
-        // copies still in flight target this CTA's shared memory: wait for
-        // them (blocks kfail .. issued-1, at most one per stage)
-        for (uint32_t k = kfail; k < issued; k++) mbar_wait(&bar[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT);
+        // this warp is done with stage k % NS
+        __syncwarp();
+        if ((threadIdx.x & 31u) == 0) mbar_arrive(&empty[k % NS]);
     }
 }
 
