@@ -23,7 +23,7 @@ _LIB = None
 
 ORDER_CUDA, ORDER_FORTRAN = 0, 1
 CS_SQRT_RT, CS_INV_SQRT3 = 0, 1
-FACE_PERIODIC, FACE_WALL, FACE_WALL_BB = 0, 1, 2
+FACE_PERIODIC, FACE_WALL, FACE_WALL_BB, FACE_FDBC = 0, 1, 2, 3
 
 
 class Lattice(ctypes.Structure):

@@ -32,6 +32,20 @@ static void launch(K kernel) {
             }
 }
 
+/* a serial launch over the grid (no OpenMP), for kernels whose threads race */
+template <typename K>
+static void launch_serial(K kernel) {
+    for (int iz = 0; iz < LZ; iz++)
+        for (int iy = 0; iy < LY; iy++)
+            for (int ix = 0; ix < LX; ix++) {
+                threadIdx.x = threadIdx.y = threadIdx.z = 0;
+                blockIdx.x = ix;
+                blockIdx.y = iy;
+                blockIdx.z = iz;
+                kernel();
+            }
+}
+
 extern "C" {
 
 int ref_lx() { return LX; }
@@ -138,6 +152,33 @@ void ref_run_trip(int nsteps, long long start_istep, int npforcing, double *f, d
         launch([&] { RRBC(f, fx, fy, fz, rho, ux, uy, uz, taut); });
         launch([&] { macrovar_BN(f, fx, fy, fz, rho, ux, uy, uz); });
     }
+}
+
+/* the step of ref_step with the finite-difference wall closure FDBC in place
+ * of RRBC (the alternative main.cu:76-77 leave commented out).  FDBC writes
+ * the extrapolated wall velocity and reads its x/z neighbours' in the same
+ * kernel, so its result depends on the order of its threads.  Run here so that
+ * every neighbour is already extrapolated: a first FDBC over a scratch copy of
+ * f leaves the extrapolated wall-row velocities in ux, uy, uz (they depend on
+ * rows 1 and 2 only), then FDBC on f rewrites them with the same values and
+ * reads only final ones. */
+void ref_step_fdbc(double *f, double *f_temp, double *rho, double *ux, double *uy, double *uz,
+                   double *fx, double *fy, double *fz, double *taut) {
+    launch([&] { forcing(fx, fy, fz); });
+    if (USE_LES) launch([&] { LES_WALE(ux, uy, uz, taut); });
+    launch([&] { collision_RR(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+    launch([&] { streaming(f, f_temp); });
+    launch([&] { BB(f, f_temp); });
+    memcpy(f, f_temp, sizeof(double) * (size_t)NPOP * LXYZ);
+    launch([&] { macrovar(f, fx, fy, fz, rho, ux, uy, uz); });
+    launch_serial([&] { FDBC(f_temp, fx, fy, fz, rho, ux, uy, uz, taut); });
+    launch_serial([&] { FDBC(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+    launch([&] { macrovar_BN(f, fx, fy, fz, rho, ux, uy, uz); });
+}
+
+void ref_run_fdbc(int nsteps, double *f, double *f_temp, double *rho, double *ux, double *uy,
+                  double *uz, double *fx, double *fy, double *fz, double *taut) {
+    for (int i = 0; i < nsteps; i++) ref_step_fdbc(f, f_temp, rho, ux, uy, uz, fx, fy, fz, taut);
 }
 
 /* rand() of this C library after srand(seed), n values (checks of the restatement) */

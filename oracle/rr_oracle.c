@@ -572,6 +572,129 @@ void orc_wale(const orc_params *P, const double *ux, const double *uy, const dou
             }
 }
 
+void orc_fdbc(const orc_params *P, double *f, double *rho, double *ux, double *uy, double *uz,
+              const double *taut) {
+    const orc_lattice *L = &P->lat;
+    const int nx = P->nx, ny = P->ny, nz = P->nz, q = L->q;
+    const long N = (long)nx * ny * nz;
+    /* (1) wall velocity from the first two rows inside: the quadratic through
+     * u = 0 on the wall half a node out, u(1) and u(2), at the wall node */
+    for (int side = 0; side < 2; side++) {
+        if (P->face[2 + side] != ORC_FACE_FDBC) continue;
+        const int iy = side ? ny - 1 : 0, dy = side ? -1 : 1;
+        for (int iz = 0; iz < nz; iz++)
+            for (int ix = 0; ix < nx; ix++) {
+                const long idx = ((long)iz * ny + iy) * nx + ix;
+                const long i1 = ((long)iz * ny + iy + dy) * nx + ix, i2 = ((long)iz * ny + iy + 2 * dy) * nx + ix;
+                ux[idx] = 2.0 / 3.0 * ux[i1] - 1.0 / 5.0 * ux[i2];
+                uy[idx] = 2.0 / 3.0 * uy[i1] - 1.0 / 5.0 * uy[i2];
+                uz[idx] = 2.0 / 3.0 * uz[i1] - 1.0 / 5.0 * uz[i2];
+            }
+    }
+    /* (2) the closure, BC.cu:162-308 */
+    for (int side = 0; side < 2; side++) {
+        if (P->face[2 + side] != ORC_FACE_FDBC) continue;
+        const int iy = side ? ny - 1 : 0;
+#pragma omp parallel for schedule(static)
+        for (int iz = 0; iz < nz; iz++)
+            for (int ix = 0; ix < nx; ix++) {
+                const long idx = ((long)iz * ny + iy) * nx + ix;
+                const double tau_eff = taut ? P->tau + taut[idx] : P->tau;
+                double dudy, dvdy, dwdy;
+                if (!side) {
+                    const long p1 = ((long)iz * ny + iy + 1) * nx + ix, p2 = ((long)iz * ny + iy + 2) * nx + ix;
+                    dudy = (-3.0 * ux[idx] + 4.0 * ux[p1] - ux[p2]) / 2.0;
+                    dvdy = (-3.0 * uy[idx] + 4.0 * uy[p1] - uy[p2]) / 2.0;
+                    dwdy = (-3.0 * uz[idx] + 4.0 * uz[p1] - uz[p2]) / 2.0;
+                } else {
+                    const long m1 = ((long)iz * ny + iy - 1) * nx + ix, m2 = ((long)iz * ny + iy - 2) * nx + ix;
+                    dudy = (3.0 * ux[idx] - 4.0 * ux[m1] + ux[m2]) / 2.0;
+                    dvdy = (3.0 * uy[idx] - 4.0 * uy[m1] + uy[m2]) / 2.0;
+                    dwdy = (3.0 * uz[idx] - 4.0 * uz[m1] + uz[m2]) / 2.0;
+                }
+                const int ixp = (ix + 1) % nx, ixm = (ix - 1 + nx) % nx;
+                const int izp = (iz + 1) % nz, izm = (iz - 1 + nz) % nz;
+                const long xp = ((long)iz * ny + iy) * nx + ixp, xm = ((long)iz * ny + iy) * nx + ixm;
+                const long zp = ((long)izp * ny + iy) * nx + ix, zm = ((long)izm * ny + iy) * nx + ix;
+                const double dudx = 0.5 * (ux[xp] - ux[xm]), dvdx = 0.5 * (uy[xp] - uy[xm]),
+                             dwdx = 0.5 * (uz[xp] - uz[xm]);
+                const double dudz = 0.5 * (ux[zp] - ux[zm]), dvdz = 0.5 * (uy[zp] - uy[zm]),
+                             dwdz = 0.5 * (uz[zp] - uz[zm]);
+                const double S110 = 0.5 * (dudy + dvdx), S101 = 0.5 * (dudz + dwdx), S011 = 0.5 * (dvdz + dwdy);
+                const double S200 = dudx, S020 = dvdy, S002 = dwdz;
+                double F[3];
+                node_force(P, N, idx, F);
+                const double fx9 = F[0], fy9 = F[1], fz9 = F[2];
+                const double u9 = ux[idx], v9 = uy[idx], w9 = uz[idx];
+                const double G3 = u9 * fx9 + v9 * fy9 + w9 * fz9;
+                const double uu = u9 / L->cs, vv = v9 / L->cs, ww = w9 / L->cs;
+                const double a110 = uu * vv, a101 = uu * ww, a011 = vv * ww, a200 = uu * uu, a020 = vv * vv,
+                             a002 = ww * ww;
+                const double a210 = a200 * vv, a201 = a200 * ww, a120 = a020 * uu, a021 = a020 * ww,
+                             a012 = a002 * vv, a102 = a002 * uu, a111 = a110 * ww;
+                double fbar[27], fir[27], sec[27], thir[27];
+                for (int ip = 0; ip < q; ip++) {
+                    const double G1 = L->cx[ip] * fx9 + L->cy[ip] * fy9 + L->cz[ip] * fz9;
+                    fbar[ip] = 0.5 * (G1 - G3) / L->rt;
+                    fir[ip] = L->H100[ip] * uu + L->H010[ip] * vv + L->H001[ip] * ww;
+                    sec[ip] = sec2(L, ip, a110, a101, a011, a200, a020, a002);
+                    thir[ip] = thir27(L, ip, a210, a201, a021, a120, a012, a102, a111);
+                }
+                /* the non-equilibrium coefficients -rho tau S and their
+                 * recursive third order (BC.cu:227-241, 265-279) */
+                double ane[13];
+                double rho9 = 1.0; /* BC.cu:213: the density the known-population balance starts from */
+                double sum_f_ps = 0.0, sum_g_in = 0.0;
+                for (int pass = 0; pass < 2; pass++) {
+                    ane[0] = -rho9 * tau_eff * S110;
+                    ane[1] = -rho9 * tau_eff * S101;
+                    ane[2] = -rho9 * tau_eff * S011;
+                    ane[3] = -rho9 * tau_eff * S200;
+                    ane[4] = -rho9 * tau_eff * S020;
+                    ane[5] = -rho9 * tau_eff * S002;
+                    ane[6] = ane[3] * vv + 2. * uu * ane[0];  /* 210 */
+                    ane[7] = ane[3] * ww + 2. * uu * ane[1];  /* 201 */
+                    ane[8] = ane[4] * uu + 2. * vv * ane[0];  /* 120 */
+                    ane[9] = ane[4] * ww + 2. * vv * ane[2];  /* 021 */
+                    ane[10] = ane[5] * uu + 2. * ww * ane[1]; /* 102 */
+                    ane[11] = ane[5] * vv + 2. * ww * ane[2]; /* 012 */
+                    ane[12] = ane[0] * ww + ane[1] * vv + ane[2] * uu;
+                    for (int ip = 0; ip < q; ip++) {
+                        /* known: the populations streamed in from inside (BC.cu:245) */
+                        const int known = side ? (L->cy[ip] > 0) : (L->cy[ip] < 0);
+                        if (pass == 0 && !known) continue;
+                        const double feq = L->w[ip] * rho9 * (1.0 + fir[ip] + 0.5 * (sec[ip] + thir[ip]));
+                        const double secneq = sec2(L, ip, ane[0], ane[1], ane[2], ane[3], ane[4], ane[5]);
+                        const double thirneq = thir27(L, ip, ane[6], ane[7], ane[9], ane[8], ane[11], ane[10], ane[12]);
+                        const double fneq = L->w[ip] * (secneq + thirneq);
+                        const double g = feq + fneq - fbar[ip] * feq;
+                        if (pass == 0) {
+                            sum_f_ps += f[ip * N + idx];
+                            sum_g_in += g;
+                        } else {
+                            f[ip * N + idx] = g;
+                        }
+                    }
+                    /* BC.cu:262: the density that balances the known populations */
+                    if (pass == 0) rho9 = sum_f_ps / sum_g_in;
+                }
+            }
+    }
+    /* (3) macrovar_BN */
+    for (int side = 0; side < 2; side++) {
+        if (P->face[2 + side] != ORC_FACE_FDBC) continue;
+        const int iy = side ? ny - 1 : 0;
+        for (int iz = 0; iz < nz; iz++)
+            for (int ix = 0; ix < nx; ix++) {
+                const long idx = ((long)iz * ny + iy) * nx + ix;
+                double fl[27], F[3];
+                for (int ip = 0; ip < q; ip++) fl[ip] = f[ip * N + idx];
+                node_force(P, N, idx, F);
+                orc_moments_node(L, F, fl, &rho[idx], &ux[idx], &uy[idx], &uz[idx]);
+            }
+    }
+}
+
 /* one reference time step, main.cu:373-409: [WALE] -> collide -> stream+BB
  * -> moments -> wall closure -> wall moments.  The wall closure is folded
  * into orc_stream_walls (it only needs the node's own populations), and the
@@ -584,6 +707,8 @@ void orc_step(const orc_params *P, orc_state *S) {
     S->f = S->ftmp;
     S->ftmp = t;
     orc_moments_all(P, S->f, S->rho, S->ux, S->uy, S->uz);
+    if (P->face[2] == ORC_FACE_FDBC || P->face[3] == ORC_FACE_FDBC)
+        orc_fdbc(P, S->f, S->rho, S->ux, S->uy, S->uz, P->les ? S->taut : NULL);
 }
 
 void orc_run(const orc_params *P, orc_state *S, int nsteps) {

@@ -38,6 +38,11 @@ extern "C" {
 #define ORC_FACE_PERIODIC 0
 #define ORC_FACE_WALL 1    /* half-way bounce-back + regularized closure */
 #define ORC_FACE_WALL_BB 2 /* half-way bounce-back only */
+/* finite-difference wall closure (FDBC, BC.cu:129-309): y faces only, x and z
+ * periodic.  Bounce-back as a wall, then every population of the wall node is
+ * rebuilt from the extrapolated wall velocity, the finite-difference strain
+ * and the density of the known populations (orc_fdbc). */
+#define ORC_FACE_FDBC 3
 
 typedef struct {
     int q;   /* 19 or 27 */
@@ -97,6 +102,20 @@ void orc_regularize_node(const orc_lattice *L, const double F[3], double *f,
 
 void orc_moments_node(const orc_lattice *L, const double F[3], const double *f, double *rho,
                       double *u, double *v, double *w);
+
+/* The finite-difference wall closure of BC.cu:129-309 (the reference launches
+ * it in place of RRBC; main.cu:76-77 keep it commented out) on every y face of
+ * kind ORC_FACE_FDBC, after the moments of all nodes.  The reference writes the
+ * extrapolated wall velocity and reads its x/z neighbours' in one kernel, an
+ * order-dependent race; the semantics here are the deterministic ones the
+ * kernel's comments state: (1) the wall-row velocity of every column is
+ * extrapolated from rows 1 and 2 (BC.cu:148-160), (2) every wall node takes
+ * its strain from those velocities, its density from the known populations
+ * and rebuilds all of its populations (BC.cu:162-308), (3) the wall-row moments
+ * are taken again (macrovar_BN, macrovar.cu:32-59).  taut: the eddy viscosity
+ * of the step (NULL for DNS). */
+void orc_fdbc(const orc_params *P, double *f, double *rho, double *ux, double *uy, double *uz,
+              const double *taut);
 
 /* one full reference time step on the whole grid */
 void orc_step(const orc_params *P, orc_state *S);

@@ -14,6 +14,10 @@ the tests never need the reference itself.
 * ``channel_ref_16x12x8_les{0,1}.npz`` -- rho, ux, uy, uz after 20 steps of
   the reference's CUDA channel kernels run on the host (oracle/_ref), from
   the reference's log-law start with its parameters.h physics.
+* ``channel_fdbc_ref_16x12x8_les{0,1}.npz`` -- the same channel with the
+  reference's finite-difference wall closure FDBC (BC.cu:129-309) in place of
+  RRBC, 20 steps from the log-law start perturbed by fdbc_start(), every wall
+  neighbour extrapolated before the closure reads it (ref_step_fdbc).
 """
 import ctypes
 import os
@@ -68,8 +72,43 @@ def channel():
                             ystar=R.ref_ystar(), steps=20)
 
 
+def fdbc_start(s, seed=11):
+    """the perturbed log-law start of the FDBC fixtures (every population and
+    all three velocity components exercised)"""
+    rng = np.random.default_rng(seed)
+    s.f *= 1.0 + 1e-3 * rng.standard_normal(s.f.shape)
+    s.uy += 1e-3 * rng.standard_normal(s.uy.shape)
+    s.uz += 1e-3 * rng.standard_normal(s.uz.shape)
+
+
+def channel_fdbc():
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    for les in (0, 1):
+        path = os.path.join(ROOT, "oracle", "_ref", f"libref_16x12x8_les{les}.so")
+        R = ctypes.CDLL(path)
+        for n in ["ref_tau", "ref_force_in_x", "ref_ustar", "ref_ystar"]:
+            getattr(R, n).restype = ctypes.c_double
+        R.ref_init_constants()
+        LX, LY, LZ = R.ref_lx(), R.ref_ly(), R.ref_lz()
+        s = O.Sim(LX, LY, LZ, tau=R.ref_tau(), force=(R.ref_force_in_x(), 0, 0), les=bool(les),
+                  faces=(0, 0, O.FACE_FDBC, O.FACE_FDBC, 0, 0))
+        s.init_channel_loglaw(R.ref_ustar(), R.ref_ystar())
+        fdbc_start(s)
+        f, rho, ux, uy, uz = s.f.copy(), s.rho.copy(), s.ux.copy(), s.uy.copy(), s.uz.copy()
+        ft = np.zeros_like(f)
+        fx, fy, fz, taut = (np.zeros_like(rho) for _ in range(4))
+        P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        R.ref_run_fdbc(20, P(f), P(ft), P(rho), P(ux), P(uy), P(uz), P(fx), P(fy), P(fz), P(taut))
+        np.savez_compressed(os.path.join(HERE, f"channel_fdbc_ref_16x12x8_les{les}.npz"), rho=rho,
+                            ux=ux, uy=uy, uz=uz, taut=taut, f_sum=f.sum(axis=0),
+                            f_wall=f[:, :, [0, LY - 1], :], tau=R.ref_tau(), fx=R.ref_force_in_x(),
+                            ustar=R.ref_ustar(), ystar=R.ref_ystar(), steps=20, seed=11)
+
+
 if __name__ == "__main__":
     tg()
     laminar()
     channel()
+    channel_fdbc()
     print("fixtures written to", HERE)

@@ -9,12 +9,16 @@
 import ctypes
 import itertools
 import os
+import sys
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
 from oracle import oracle as O
+
+sys.path.insert(0, GOLDEN)
+from make_golden import fdbc_start  # noqa: E402
 
 
 @pytest.mark.parametrize("q,order", [(27, O.ORDER_CUDA), (27, O.ORDER_FORTRAN), (19, O.ORDER_FORTRAN)])
@@ -119,6 +123,58 @@ def test_channel_matches_reference_live(les):
     assert np.array_equal(s.f, f)
     for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
         assert np.array_equal(getattr(s, k), a), k
+
+
+@pytest.mark.parametrize("les", [0, 1])
+def test_fdbc_matches_reference_fixture(les):
+    """FDBC channel: the oracle against the reference's kernels' committed
+    output (tests/golden/make_golden.py channel_fdbc), bit for bit."""
+    g = np.load(os.path.join(GOLDEN, f"channel_fdbc_ref_16x12x8_les{les}.npz"))
+    s = O.Sim(16, 12, 8, q=27, order=O.ORDER_CUDA, cs_mode=O.CS_SQRT_RT, tau=float(g["tau"]),
+              force=(float(g["fx"]), 0.0, 0.0), les=bool(les), cw=0.5,
+              faces=(0, 0, O.FACE_FDBC, O.FACE_FDBC, 0, 0))
+    s.init_channel_loglaw(float(g["ustar"]), float(g["ystar"]))
+    fdbc_start(s, int(g["seed"]))
+    s.run(int(g["steps"]))
+    for k in ("rho", "ux", "uy", "uz"):
+        assert np.array_equal(getattr(s, k), g[k]), k
+    assert np.array_equal(s.f.sum(axis=0), g["f_sum"])
+    assert np.array_equal(s.f[:, :, [0, 11], :], g["f_wall"])
+    if les:
+        assert np.array_equal(s.taut, g["taut"])
+
+
+@pytest.mark.parametrize("les", [0, 1])
+def test_fdbc_matches_reference_live(les):
+    """The finite-difference wall closure (FDBC, BC.cu:129-309, in place of RRBC)
+    of the oracle against the reference's own FDBC kernel, bit for bit, with
+    every wall neighbour extrapolated before the closure reads it."""
+    R = _ref_lib(les)
+    s = O.Sim(16, 12, 8, q=27, order=O.ORDER_CUDA, cs_mode=O.CS_SQRT_RT, tau=R.ref_tau(),
+              force=(R.ref_force_in_x(), 0.0, 0.0), les=bool(les), cw=0.5,
+              faces=(0, 0, O.FACE_FDBC, O.FACE_FDBC, 0, 0))
+    s.init_channel_loglaw(R.ref_ustar(), R.ref_ystar())
+    rng = np.random.default_rng(11)
+    s.f *= 1.0 + 1e-3 * rng.standard_normal(s.f.shape)
+    s.uy += 1e-3 * rng.standard_normal(s.uy.shape)
+    s.uz += 1e-3 * rng.standard_normal(s.uz.shape)
+    f, rho, ux, uy, uz = (a.copy() for a in (s.f, s.rho, s.ux, s.uy, s.uz))
+    ft, fx, fy, fz, taut = (np.zeros_like(a) for a in (f, rho, rho, rho, rho))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    R.ref_run_fdbc(5, P(f), P(ft), P(rho), P(ux), P(uy), P(uz), P(fx), P(fy), P(fz), P(taut))
+    s.run(5)
+    assert np.array_equal(s.f, f)
+    for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
+        assert np.array_equal(getattr(s, k), a), k
+    # one more step from this state with RRBC instead: the two closures
+    # differ on the wall rows only
+    w = _channel_sim(les, R.ref_tau(), R.ref_force_in_x())
+    w.f, w.rho, w.ux, w.uy, w.uz, w.taut = (a.copy() for a in (s.f, s.rho, s.ux, s.uy, s.uz, s.taut))
+    s.run(1)
+    w.run(1)
+    assert np.array_equal(s.f[:, :, 1:-1, :], w.f[:, :, 1:-1, :])
+    for y in (0, -1):
+        assert np.abs(s.f[:, :, y, :] - w.f[:, :, y, :]).max() > 1e-9
 
 
 def _laminar_golden(step):
