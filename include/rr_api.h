@@ -51,7 +51,17 @@ typedef enum { RR_STORE_F64 = 0, RR_STORE_F32 = 1, RR_STORE_F16 = 2, RR_STORE_BF
 typedef enum {
     RR_FACE_PERIODIC = 0,
     RR_FACE_WALL = 1,    /* half-way bounce-back + regularized closure (RRBC) */
-    RR_FACE_WALL_BB = 2  /* half-way bounce-back only */
+    RR_FACE_WALL_BB = 2, /* half-way bounce-back only */
+    /* finite-difference wall closure (FDBC, RR27V33_code_DNS_LES/BC.cu:129-309,
+     * the alternative main.cu:76-77 leave commented out): y faces only, x and
+     * z periodic, wall at rest, ly >= 4, RR collision.  Every population of
+     * the wall node is rebuilt from the wall velocity extrapolated from rows
+     * 1 and 2 inward, the finite-difference strain and the density of the
+     * populations streamed in from inside.  The velocities of all wall nodes
+     * are extrapolated before any closure reads its neighbours' (the
+     * reference's single kernel races there).  With WALE: the two-pass method
+     * only (lx >= 3). */
+    RR_FACE_FDBC = 3
 } rr_face;
 
 /* velocity ordering of populations crossing the API (rr_init_state, rr_get_f,

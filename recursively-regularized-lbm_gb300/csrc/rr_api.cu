@@ -81,7 +81,7 @@ rr_status validate(const rr_params *p) {
         return fail(RR_ERR_INVALID, "D3Q19 populations exist only in the Fortran ordering");
     const int n3[3] = {p->lx, p->ly, p->lz};
     for (int f = 0; f < 6; f++) {
-        if (p->face[f] < RR_FACE_PERIODIC || p->face[f] > RR_FACE_WALL_BB)
+        if (p->face[f] < RR_FACE_PERIODIC || p->face[f] > RR_FACE_FDBC)
             return fail(RR_ERR_INVALID, "face[%d] = %d unknown", f, p->face[f]);
         if (p->face[f] != RR_FACE_PERIODIC && n3[f / 2] < 2)
             return fail(RR_ERR_INVALID, "a wall on face %d needs at least 2 nodes across", f);
@@ -101,6 +101,23 @@ rr_status validate(const rr_params *p) {
         return fail(RR_ERR_UNSUPPORTED, "trip forcing needs D3Q27 and lx >= 3");
     if (p->collision != RR_COLL_RR && p->collision != RR_COLL_BGK)
         return fail(RR_ERR_INVALID, "collision = %d unknown", p->collision);
+    const bool fdbc = p->face[2] == RR_FACE_FDBC || p->face[3] == RR_FACE_FDBC;
+    for (int f : {0, 1, 4, 5})
+        if (p->face[f] == RR_FACE_FDBC)
+            return fail(RR_ERR_UNSUPPORTED, "the finite-difference closure is for the y faces only (face %d)", f);
+    if (fdbc) {
+        // BC.cu:129-309: x and z periodic, walls at rest, rows 1 and 2 inside
+        if (p->face[0] != RR_FACE_PERIODIC || p->face[4] != RR_FACE_PERIODIC)
+            return fail(RR_ERR_UNSUPPORTED, "the finite-difference closure needs periodic x and z");
+        for (int f = 2; f < 4; f++)
+            if (p->face[f] == RR_FACE_FDBC && (p->uwall[f][0] != 0.0 || p->uwall[f][1] != 0.0 || p->uwall[f][2] != 0.0))
+                return fail(RR_ERR_UNSUPPORTED, "the finite-difference closure takes walls at rest (face %d)", f);
+        if (p->ly < 4) return fail(RR_ERR_UNSUPPORTED, "the finite-difference closure needs ly >= 4");
+        if (p->collision != RR_COLL_RR)
+            return fail(RR_ERR_UNSUPPORTED, "the finite-difference closure needs the RR collision");
+        if (p->use_les && p->lx < 3)
+            return fail(RR_ERR_UNSUPPORTED, "WALE with the finite-difference closure needs lx >= 3");
+    }
     if (p->collision == RR_COLL_BGK) {
         if (p->q != 27 || p->use_les || p->lx < 3 || p->trip_steps > 0)
             return fail(RR_ERR_UNSUPPORTED, "the BGK collision needs D3Q27, DNS, lx >= 3 and no trip forcing");
@@ -153,6 +170,37 @@ const double *readout_field(rr_solver *s) {
     return (s->ffield && s->istep >= 1 && s->istep < s->p.trip_steps) ? rr::trip_slot(s, s->istep) : nullptr;
 }
 
+// the readout of the state after the last step from the previous buffer:
+// populations (fo, reference layout) and/or moments; the wall rows of the
+// finite-difference closure's faces come from its own kernel
+cudaError_t readout_state(rr_solver *s, double *fo, double *rho, double *ux, double *uy, double *uz) {
+    const void *fin = s->buf[1 - s->cur];
+    const double *ff = readout_field(s);
+    cudaError_t e = s->ops->readout(s->p.q, rr::has_force(s->p), fin, s->g, s->p.force, fo, s->g.n, s->pos, rho, ux,
+                                    uy, uz, ff, s->stream);
+    if (e != cudaSuccess || !s->fdbc) return e;
+    rr::FdbcCall fc{};
+    fc.q = s->p.q;
+    fc.force = rr::has_force(s->p);
+    fc.mode = 3;
+    fc.fin = fin;
+    fc.g = &s->g;
+    fc.tau = s->p.tau;
+    fc.F = s->p.force;
+    fc.status = s->status;
+    fc.ffp = ff;
+    fc.wt = s->fdbc_wt[1 - s->cur];
+    fc.fo = fo;
+    fc.fo_stride = s->g.n;
+    fc.pos = s->pos;
+    fc.rho = rho;
+    fc.ux = ux;
+    fc.uy = uy;
+    fc.uz = uz;
+    fc.faces = s->fdbc;
+    return s->ops->fdbc(fc, s->stream);
+}
+
 // rho, u (and taut) of the current state into aux
 rr_status readout_macros(rr_solver *s, bool want_taut) {
     rr_status st = ensure_aux(s);
@@ -160,8 +208,7 @@ rr_status readout_macros(rr_solver *s, bool want_taut) {
     const size_t n = s->g.n;
     double *rho = s->aux, *ux = rho + n, *uy = ux + n, *uz = uy + n, *tt = uz + n;
     // the previous buffer holds the post-collision state the last step read
-    RR_CK(s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, nullptr, 0,
-                          s->pos, rho, ux, uy, uz, readout_field(s), s->stream));
+    RR_CK(readout_state(s, nullptr, rho, ux, uy, uz));
     if (want_taut) RR_CK(rr::launch_wale(s->g, s->p.cw, ux, uy, uz, tt, s->stream));
     return RR_OK;
 }
@@ -255,10 +302,42 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         ffp = trip_slot(s, i + 1);
         ffc = trip_slot(s, i + 2);
     }
+    rr::FdbcCall fc{};
+    if (s->fdbc) {
+        fc.q = s->p.q;
+        fc.force = force;
+        fc.fin = fin;
+        fc.fout = fout;
+        fc.g = &s->g;
+        fc.om1 = 1.0 - 1.0 / s->p.tau;
+        fc.tau = s->p.tau;
+        fc.cw = s->p.cw;
+        fc.F = s->p.force;
+        fc.status = s->status;
+        fc.ffp = ffp;
+        fc.ffc = ffc;
+        fc.ubuf = s->ubuf;
+        const int in = fin == s->buf[1] ? 1 : 0;
+        fc.wt = s->fdbc_wt[in];
+        fc.wt_out = s->fdbc_wt[1 - in];
+        fc.faces = s->fdbc;
+    }
     if (s->p.use_les) {
+        if (s->fdbc) {
+            // the wall rows' velocities are the closure's before tau_t reads them
+            RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
+                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, 1, st));
+            fc.mode = 1;
+            RR_CK(s->ops->fdbc(fc, st));
+            RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
+                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, 2, st));
+            fc.mode = 2;
+            RR_CK(s->ops->fdbc(fc, st));
+            return RR_OK;
+        }
         if ((s->les_method == RR_LES_TWO_PASS || ffp) && s->ubuf)
             RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
-                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, st));
+                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, 0, st));
         else
             RR_CK(s->ops->step_les(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
                                    s->tile, st));
@@ -271,6 +350,10 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
     } else {
         RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status, s->all,
                            s->block, st));
+    }
+    if (s->fdbc) {
+        fc.mode = 0;
+        RR_CK(s->ops->fdbc(fc, st));
     }
     return RR_OK;
 }
@@ -330,6 +413,9 @@ size_t rr_bytes_for(const rr_params *p) {
     if (p->lx >= 3) b += 2 * sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
     if (rr::staged_ok(*p, elem)) b += sizeof(uint32_t) * (size_t)(2 * p->lz + 2 * p->ly);
     if (p->trip_steps > 0) b += 6 * padded_stride(n) * sizeof(double);
+    // wall tau_t of WALE with the finite-difference closure: two slots
+    if (p->use_les && (p->face[2] == RR_FACE_FDBC || p->face[3] == RR_FACE_FDBC))
+        b += 4 * (size_t)p->lx * p->lz * sizeof(double);
     return b;
 }
 
@@ -483,6 +569,18 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     } else {
         s->les_method = RR_LES_FUSED;
     }
+    s->fdbc = (p->face[2] == RR_FACE_FDBC ? 1u : 0u) | (p->face[3] == RR_FACE_FDBC ? 2u : 0u);
+    if (s->fdbc && p->use_les) {
+        const size_t slot = 2 * (size_t)p->lx * p->lz;
+        if (cudaMalloc(&s->fdbc_wt_mem, 2 * slot * sizeof(double)) != cudaSuccess ||
+            cudaMemset(s->fdbc_wt_mem, 0, 2 * slot * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of wall tau_t", 2 * slot * sizeof(double)));
+        }
+        s->fdbc_wt[0] = s->fdbc_wt_mem;
+        s->fdbc_wt[1] = s->fdbc_wt_mem + slot;
+        s->bytes += 2 * slot * sizeof(double);
+    }
     if (p->trip_steps > 0) {
         const size_t fb = 6 * (size_t)g.stride * sizeof(double);
         if (cudaMalloc(&s->ffield, fb) != cudaSuccess) {
@@ -520,6 +618,7 @@ rr_status rr_destroy(rr_solver *s) {
     cudaFree(s->ubuf);
     cudaFree(s->frow_list);
     cudaFree(s->ffield);
+    cudaFree(s->fdbc_wt_mem);
     if (s->side) {
         cudaStreamSynchronize(s->side);
         cudaStreamDestroy(s->side);
@@ -575,6 +674,9 @@ rr_status init_state_at(rr_solver *s, const double *f, const double *rho, const 
     if (e == cudaSuccess)
         e = s->ops->upload(s->p.q, rr::has_force(s->p), s->buf[0], s->g, s->p.tau, s->p.force, d_f, n,
                            s->pos, d_rho, d_ux, d_uy, d_uz, s->p.use_les ? d_tt : nullptr, ff, s->stream);
+    // the finite-difference closure of step istep0 + 1 takes that step's tau_t
+    // at the wall nodes: kept with the buffer the upload wrote
+    if (e == cudaSuccess && s->fdbc_wt[0]) e = rr::launch_wall_rows(s->g, d_tt, s->fdbc_wt[0], s->stream);
     cudaError_t e2 = cudaFreeAsync(tmp, s->stream);
     if (e != cudaSuccess) return fail(RR_ERR_CUDA, "state upload failed: %s", cudaGetErrorString(e));
     if (e2 != cudaSuccess) return fail(RR_ERR_CUDA, "cudaFreeAsync: %s", cudaGetErrorString(e2));
@@ -676,8 +778,7 @@ rr_status rr_get_f(rr_solver *s, double *f, int where) {
         RR_CK(cudaMallocAsync(&tmp, nf * sizeof(double), s->stream));
         dst = tmp;
     }
-    cudaError_t e = s->ops->readout(s->p.q, rr::has_force(s->p), s->buf[1 - s->cur], s->g, s->p.force, dst,
-                                    n, s->pos, nullptr, nullptr, nullptr, nullptr, readout_field(s), s->stream);
+    cudaError_t e = readout_state(s, dst, nullptr, nullptr, nullptr, nullptr);
     if (e == cudaSuccess && tmp) e = cudaMemcpyAsync(f, tmp, nf * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
     if (tmp) cudaFreeAsync(tmp, s->stream);
     if (e != cudaSuccess) return fail(RR_ERR_CUDA, "readout failed: %s", cudaGetErrorString(e));

@@ -244,4 +244,21 @@ cudaError_t launch_trip_force(double *ff, unsigned long long stride, int LX, int
     return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(256)
+wall_rows_kernel(int nx, int ny, int nz, const double *__restrict__ field, double *__restrict__ out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t per = (uint32_t)nx * (uint32_t)nz;
+    if (t >= 2u * per) return;
+    const uint32_t side = t / per, c = t - side * per;
+    const uint32_t z = c / (uint32_t)nx, x = c - z * (uint32_t)nx;
+    const uint32_t y = side ? (uint32_t)ny - 1u : 0u;
+    out[t] = field[(z * (uint32_t)ny + y) * (uint32_t)nx + x];
+}
+
+cudaError_t launch_wall_rows(const Geom &g, const double *field, double *out, cudaStream_t st) {
+    const uint32_t m = 2u * (uint32_t)g.nx * (uint32_t)g.nz;
+    wall_rows_kernel<<<(m + 255) / 256, 256, 0, st>>>(g.nx, g.ny, g.nz, field, out);
+    return cudaGetLastError();
+}
+
 } // namespace rr

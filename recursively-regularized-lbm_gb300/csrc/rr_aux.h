@@ -29,4 +29,7 @@ cudaError_t launch_accumulate(int m, const double *prof, double *acc, cudaStream
 cudaError_t launch_trip_force(double *ff, unsigned long long stride, int LX, int LY, int LZ, int trip, double amp,
                               double phase, const double F[3], cudaStream_t st);
 
+// the y = 0 and y = ny-1 rows of a field (N doubles) into out[side][z][x]
+cudaError_t launch_wall_rows(const Geom &g, const double *field, double *out, cudaStream_t st);
+
 } // namespace rr

@@ -110,7 +110,7 @@ rr_status build_tables(rr_batch *b) {
     // group_bytes of population buffers
     std::vector<Class> big;
     for (rr_solver *s : b->members) {
-        if (!rr::tile_step(s)) {
+        if (!rr::batchable(s)) {
             b->others.push_back(s);
             continue;
         }
@@ -419,6 +419,7 @@ rr_status rr_batch_add(rr_batch *b, rr_solver *s) {
     BK(cudaStreamSynchronize(s->stream)); // the solver's own pending work
     if (s->cur != b->parity) {
         std::swap(s->buf[0], s->buf[1]);
+        std::swap(s->fdbc_wt[0], s->fdbc_wt[1]);
         s->cur = b->parity;
         rr::drop_graph(s); // captured with the old labels
     }
@@ -577,6 +578,8 @@ rr_status rr_set_launch(rr_solver *s, int rows_group, const int *les_method, con
             return rr_internal_error(RR_ERR_INVALID, "les_method = %d unknown", method);
         if (method == RR_LES_TWO_PASS && !s->ubuf)
             return rr_internal_error(RR_ERR_INVALID, "the two-pass WALE step needs use_les and lx >= 3");
+        if (method == RR_LES_FUSED && s->fdbc && s->p.use_les)
+            return rr_internal_error(RR_ERR_UNSUPPORTED, "WALE with the finite-difference closure is two-pass only");
     }
     if (rows_group < 32 || rows_group % 32 != 0 || rows_group > 4096)
         return rr_internal_error(RR_ERR_INVALID, "rows_group = %d, must be a multiple of 32 in [32, 4096]", rows_group);
@@ -751,7 +754,7 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run) {
     // 1. threads per CTA and CTAs per SM of the persistent launch
     int occ_max = 0;
     for (rr_solver *s : b->members)
-        if (rr::tile_step(s)) occ_max = std::max(occ_max, s->ops->batch_occupancy(s->p.q, rr::has_force(s->p), 128));
+        if (rr::batchable(s)) occ_max = std::max(occ_max, s->ops->batch_occupancy(s->p.q, rr::has_force(s->p), 128));
     struct Shape {
         int block, cps, order;
     };

@@ -23,6 +23,29 @@ struct StepRange {
     const uint32_t *list;
 };
 
+// one launch of the finite-difference wall closure (rr_fdbc.cuh) over the
+// FDBC y faces: after the step kernels, from the same input buffer
+struct FdbcCall {
+    int q;
+    bool force;
+    int mode;                 // 0 DNS step, 1 / 2 the WALE passes, 3 readout
+    const void *fin;
+    void *fout;
+    const Geom *g;
+    double om1, tau, cw;
+    const double *F;          // uniform force (3)
+    int *status;
+    const double *ffp, *ffc;  // per-node forces (trip forcing) or NULL
+    void *ubuf;               // WALE velocity field
+    double *wt;               // WALE tau_t of the wall nodes, 2 nz nx (NULL for DNS): of fin's collision
+    double *wt_out;           // ... and of this step's collision (mode 2)
+    double *fo;               // readout: populations (or NULL) ...
+    unsigned long long fo_stride;
+    const int *pos;
+    double *rho, *ux, *uy, *uz; // ... and moments (or NULL)
+    uint32_t faces;           // bit 0: y-lo is FDBC, bit 1: y-hi
+};
+
 struct Ops {
     size_t elem_bytes;
     // one fused time step over the nodes of `r`: fin -> fout
@@ -63,10 +86,11 @@ struct Ops {
                             double tau, double cw, const double F[3], int *status,
                             const LesTile &tile, cudaStream_t st);
     // the same step in two tile launches (needs nx >= 3): velocities into ubuf
-    // (3 arrays of g.stride in the compute type), then tau_t + collision
+    // (3 arrays of g.stride in the compute type), then tau_t + collision;
+    // pass 1 or 2 launches that pass alone, 0 both
     cudaError_t (*les2)(int q, bool force, const void *fin, void *fout, const Geom &g, double tau, double cw,
                         const double F[3], int *status, const uint32_t *edges, uint32_t nedges, int rows_group,
-                        void *ubuf, const double *ffp, const double *ffc, cudaStream_t st);
+                        void *ubuf, const double *ffp, const double *ffc, int pass, cudaStream_t st);
     // post-stream populations / macroscopic fields from the post-collision buffer
     cudaError_t (*readout)(int q, bool force, const void *fin, const Geom &g, const double F[3],
                            double *fo, unsigned long long fo_stride, const int *pos, double *rho,
@@ -76,6 +100,8 @@ struct Ops {
                           const double F[3], const double *fi, unsigned long long fi_stride,
                           const int *pos, const double *rho, const double *ux, const double *uy,
                           const double *uz, const double *taut, const double *ff, cudaStream_t st);
+    // the finite-difference wall closure of the FDBC faces
+    cudaError_t (*fdbc)(const FdbcCall &c, cudaStream_t st);
 };
 
 const Ops &ops_f64();

@@ -77,6 +77,11 @@ struct rr_solver {
     double *ffield = nullptr;        // trip forcing: the force fields of two steps (2 x 3 arrays of g.stride)
     TripRand trip_rng;
     double trip_phase = 0.0;
+    uint32_t fdbc = 0;               // finite-difference wall closure: bit 0 y-lo, bit 1 y-hi
+    // WALE with FDBC: tau_t of the wall nodes (2 nz nx each) of the collision
+    // that wrote buf[b] in slot b (swapped with the buffers)
+    double *fdbc_wt[2] = {nullptr, nullptr};
+    double *fdbc_wt_mem = nullptr;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -88,6 +93,9 @@ namespace rr {
 bool has_force(const rr_params &p);
 // the step kind of a solver: the tile step (one launch, batchable) or not
 inline bool tile_step(const rr_solver *s) { return !s->p.use_les && s->p.lx >= 3 && !s->g.bgk; }
+// a tile-step solver the persistent batch kernel can step (its whole step is
+// the one tile launch: no finite-difference closure pass after it)
+inline bool batchable(const rr_solver *s) { return tile_step(s) && !s->fdbc; }
 // the staged step applies: DNS, at least 3 nodes on every axis, rows a
 // multiple of 16 bytes (bulk copies)
 inline bool staged_ok(const rr_params &p, size_t elem) {

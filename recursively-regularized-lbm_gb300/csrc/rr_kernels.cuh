@@ -29,7 +29,9 @@
 
 namespace rr {
 
-enum FaceKind : int { FACE_PERIODIC = 0, FACE_WALL = 1, FACE_WALL_BB = 2 };
+// FACE_FDBC: bounce-back inside the step kernels, then the wall rows are
+// rebuilt by fdbc_kernel (rr_fdbc.cuh)
+enum FaceKind : int { FACE_PERIODIC = 0, FACE_WALL = 1, FACE_WALL_BB = 2, FACE_FDBC = 3 };
 
 struct Geom {
     int nx, ny, nz;
@@ -654,6 +656,41 @@ __global__ void __launch_bounds__(256, batch_min_blocks<S>()) batch_kernel(const
     }
 }
 
+// a readout's outputs of one node from its post-stream deviations d
+template <class LT, typename T>
+__device__ __forceinline__ void readout_node(const T (&d)[LT::Q], uint32_t idx, bool bgk, double Fx_, double Fy_,
+                                             double Fz_, double *__restrict__ fo, unsigned long long fo_stride,
+                                             const int *__restrict__ pos, double *__restrict__ rho,
+                                             double *__restrict__ ux_o, double *__restrict__ uy_o,
+                                             double *__restrict__ uz_o) {
+    if (fo) {
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            fo[(unsigned long long)pos[i] * fo_stride + idx] = LT::w(i) * (1.0 + double(d[i]));
+        });
+    }
+    if (rho) {
+        // moments in FP64 from the stored state (macrovar.cu:18-28)
+        double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const double fv = LT::w(i) * (1.0 + double(d[i]));
+            r += fv;
+            if constexpr (LT::cx(i) > 0) jx += fv;
+            if constexpr (LT::cx(i) < 0) jx -= fv;
+            if constexpr (LT::cy(i) > 0) jy += fv;
+            if constexpr (LT::cy(i) < 0) jy -= fv;
+            if constexpr (LT::cz(i) > 0) jz += fv;
+            if constexpr (LT::cz(i) < 0) jz -= fv;
+        });
+        rho[idx] = r;
+        // BGK: the incompressible velocity, not divided by rho
+        ux_o[idx] = bgk ? jx + 0.5 * Fx_ : (jx + 0.5 * Fx_) / r;
+        uy_o[idx] = bgk ? jy + 0.5 * Fy_ : (jy + 0.5 * Fy_) / r;
+        uz_o[idx] = bgk ? jz + 0.5 * Fz_ : (jz + 0.5 * Fz_) / r;
+    }
+}
+
 // Readout: the reference's post-stream state after the last step, from the
 // previous post-collision buffer.  Writes FP64 f (reference layout, ordering
 // given by pos: internal population i goes to output population pos[i]) and/or the
@@ -678,32 +715,7 @@ readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double
     pull<LT>(fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
     const T Fx = T(Fx_), Fy = T(Fy_), Fz = T(Fz_);
     if (g.wallmask && any_wall(x, y, z, g)) wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
-    if (fo) {
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            fo[(unsigned long long)pos[i] * fo_stride + idx] = LT::w(i) * (1.0 + double(d[i]));
-        });
-    }
-    if (rho) {
-        // moments in FP64 from the stored state (macrovar.cu:18-28)
-        double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            const double fv = LT::w(i) * (1.0 + double(d[i]));
-            r += fv;
-            if constexpr (LT::cx(i) > 0) jx += fv;
-            if constexpr (LT::cx(i) < 0) jx -= fv;
-            if constexpr (LT::cy(i) > 0) jy += fv;
-            if constexpr (LT::cy(i) < 0) jy -= fv;
-            if constexpr (LT::cz(i) > 0) jz += fv;
-            if constexpr (LT::cz(i) < 0) jz -= fv;
-        });
-        rho[idx] = r;
-        // BGK: the incompressible velocity, not divided by rho
-        ux_o[idx] = g.bgk ? jx + 0.5 * Fx_ : (jx + 0.5 * Fx_) / r;
-        uy_o[idx] = g.bgk ? jy + 0.5 * Fy_ : (jy + 0.5 * Fy_) / r;
-        uz_o[idx] = g.bgk ? jz + 0.5 * Fz_ : (jz + 0.5 * Fz_) / r;
-    }
+    readout_node<LT, T>(d, idx, g.bgk != 0, Fx_, Fy_, Fz_, fo, fo_stride, pos, rho, ux_o, uy_o, uz_o);
 }
 
 // State upload: populations in the reference's post-stream form (FP64,

@@ -17,7 +17,7 @@ LIBPATH = os.path.join(_HERE, "librrlbm.so")
 
 STORE_F64, STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2, 3
 STORAGE = {"f64": STORE_F64, "f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
-FACE_PERIODIC, FACE_WALL, FACE_WALL_BB = 0, 1, 2
+FACE_PERIODIC, FACE_WALL, FACE_WALL_BB, FACE_FDBC = 0, 1, 2, 3
 COLL_RR, COLL_BGK = 0, 1
 ROUND_NEAREST, ROUND_STOCHASTIC = 0, 1
 ORDER_CUDA, ORDER_FORTRAN = 0, 1

@@ -66,6 +66,49 @@ def test_invalid_faces_rejected():
         rrlbm.Solver(p)
 
 
+def _fdbc_channel(**kw):
+    p, _ = presets.channel(nx=16, ny=12, nz=8, les=False, variant="config")
+    p.face[2] = p.face[3] = rrlbm.FACE_FDBC
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+@pytest.mark.parametrize("change,msg", [
+    (lambda p: (p.face.__setitem__(0, rrlbm.FACE_FDBC), p.face.__setitem__(1, rrlbm.FACE_FDBC)), "y faces only"),
+    (lambda p: (p.face.__setitem__(0, rrlbm.FACE_WALL), p.face.__setitem__(1, rrlbm.FACE_WALL)), "periodic x and z"),
+    (lambda p: p.uwall[3].__setitem__(0, 0.05), "walls at rest"),
+    (lambda p: setattr(p, "ly", 3), "ly >= 4"),
+    (lambda p: setattr(p, "collision", rrlbm.COLL_BGK), "RR collision"),
+    (lambda p: (setattr(p, "use_les", 1), setattr(p, "lx", 2)), "lx >= 3"),
+])
+def test_fdbc_unsupported_combinations_rejected(change, msg):
+    """the finite-difference closure (BC.cu:129-309) is defined for y walls at
+    rest with x and z periodic, at least rows 1 and 2 inside"""
+    p = _fdbc_channel()
+    change(p)
+    with pytest.raises(rrlbm.RRError) as e:
+        rrlbm.Solver(p)
+    assert e.value.code == 4 and msg in str(e.value), str(e.value)
+    assert rrlbm.bytes_for(p) == 0
+
+
+def test_fdbc_face_kind_range():
+    p = _fdbc_channel()
+    p.face[2] = p.face[3] = 4
+    with pytest.raises(rrlbm.RRError) as e:
+        rrlbm.Solver(p)
+    assert e.value.code == 1 and "unknown" in str(e.value)
+
+
+def test_fdbc_bytes_for_counts_wall_slots():
+    p = _fdbc_channel(use_les=1)
+    q = _fdbc_channel(use_les=1)
+    q.face[2] = q.face[3] = rrlbm.FACE_WALL
+    assert rrlbm.bytes_for(p) - rrlbm.bytes_for(q) == 4 * 16 * 8 * 8
+    assert rrlbm.bytes_for(_fdbc_channel()) == rrlbm.bytes_for(_fdbc_channel(face=q.face))
+
+
 def test_bytes_for():
     p, _ = presets.cavity(n=128, storage="f16")
     b = rrlbm.bytes_for(p)
