@@ -51,6 +51,9 @@ WORKLOADS = {
     "cavity128_f64": dict(kind="cavity", n=128, storage="f64", Re=1000.0, U=0.1),
     "cavity128_bf16": dict(kind="cavity", n=128, storage="bf16", Re=1000.0, U=0.1),
     "channel_les_f16": dict(kind="channel", storage="f16"),
+    "channel_dns_f16": dict(kind="channel", storage="f16", les=False),
+    "channel_fdbc_f16": dict(kind="channel", storage="f16", les=False, fdbc=True),
+    "channel_les_fdbc_f16": dict(kind="channel", storage="f16", fdbc=True),
     "tg100_f64": dict(kind="tg", storage="f64"),
     "tg128_f16": dict(kind="tg128", storage="f16"),
     "tg128_bgk_f16": dict(kind="tg128", storage="f16", bgk=True),
@@ -65,7 +68,11 @@ def make(wl):
     if w["kind"] == "cavity":
         return presets.cavity(n=w["n"], Re=w["Re"], U=w["U"], storage=w["storage"], variant="config")
     if w["kind"] == "channel":
-        return presets.channel(storage=w["storage"], les=True, variant="config")
+        p, st = presets.channel(storage=w["storage"], les=w.get("les", True), variant="config")
+        if w.get("fdbc"):
+            import rrlbm
+            p.face[2] = p.face[3] = rrlbm.FACE_FDBC
+        return p, st
     if w["kind"] == "tg128":
         p, st = presets.taylor_green(L=128, nz=128, tau=0.6, Ma=0.05, storage=w["storage"])
         if w.get("bgk"):
@@ -82,7 +89,10 @@ def describe(wl, p, storage):
         return (f"lid-driven cavity {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Re=1000, lid 0.1 +x on y-hi, "
                 f"bounce-back + regularized closure on 6 faces, {storage} storage")
     if kind == "channel":
-        return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 RR + WALE (C_w=0.5), Re_tau=180, walls y, periodic x/z, "
+        w = WORKLOADS[wl]
+        model = "RR + WALE (C_w=0.5)" if w.get("les", True) else "RR DNS"
+        walls = "finite-difference closure (FDBC)" if w.get("fdbc") else "bounce-back + regularized closure"
+        return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 {model}, Re_tau=180, walls y ({walls}), periodic x/z, "
                 f"body force, {storage} storage")
     ma = 0.05 if kind == "tg128" else 0.01
     coll = "BGK" if WORKLOADS[wl].get("bgk") else "RR"
@@ -264,9 +274,12 @@ def run_gpu(args, rank, world, local_rank):
     s = rrlbm.Solver(p)
     set_dns(s, args.dns)
     # rr kernel launches per step: tile step 1; staged step 2 (interior +
-    # face rows); WALE two-pass 2, fused 1
+    # face rows); WALE two-pass 2, fused 1; the finite-difference closure one
+    # more per pass
     les_method, dns_method = s.launch()[1], s.stage()[0]
     launches_per_step = (2 if les_method == 1 else 1) if p.use_les else (2 if dns_method == 1 else 1)
+    if rrlbm.FACE_FDBC in (p.face[2], p.face[3]):
+        launches_per_step += 2 if p.use_les else 1
     s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
     stream = torch.cuda.ExternalStream(s.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

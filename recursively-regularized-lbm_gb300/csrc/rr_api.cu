@@ -322,17 +322,31 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         fc.wt_out = s->fdbc_wt[1 - in];
         fc.faces = s->fdbc;
     }
+    // the closure's kernel beside a tile launch, which leaves the closure's
+    // rows alone: on the side stream, launched first so that its CTAs are
+    // resident before the tile step fills the SMs
+    auto beside = [&](int mode, auto &&main) -> rr_status {
+        fc.mode = mode;
+        RR_CK(cudaEventRecord(s->fork, st));
+        RR_CK(cudaStreamWaitEvent(s->side, s->fork, 0));
+        RR_CK(s->ops->fdbc(fc, s->side));
+        rr_status r = main();
+        if (r != RR_OK) return r;
+        RR_CK(cudaEventRecord(s->join, s->side));
+        RR_CK(cudaStreamWaitEvent(st, s->join, 0));
+        return RR_OK;
+    };
     if (s->p.use_les) {
         if (s->fdbc) {
             // the wall rows' velocities are the closure's before tau_t reads them
-            RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
-                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, 1, st));
-            fc.mode = 1;
-            RR_CK(s->ops->fdbc(fc, st));
-            RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
-                               s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, 2, st));
-            fc.mode = 2;
-            RR_CK(s->ops->fdbc(fc, st));
+            for (int pass = 1; pass <= 2; pass++) {
+                rr_status r = beside(pass, [&]() -> rr_status {
+                    RR_CK(s->ops->les2(s->p.q, force, fin, fout, s->g, s->p.tau, s->p.cw, s->p.force, s->status,
+                                       s->edge_list, s->nedges, s->rows_group, s->ubuf, ffp, ffc, pass, st));
+                    return RR_OK;
+                });
+                if (r != RR_OK) return r;
+            }
             return RR_OK;
         }
         if ((s->les_method == RR_LES_TWO_PASS || ffp) && s->ubuf)
@@ -345,12 +359,17 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         RR_CK(s->ops->staged(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
                              s->frow_list, s->nfrows, s->stage_rows, s->stages, st, s->side, s->fork, s->join));
     } else if (s->p.lx >= 3) {
-        RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
-                           s->edge_list, s->nedges, s->rows_group, ffp, ffc, st));
+        auto tile = [&]() -> rr_status {
+            RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
+                               s->edge_list, s->nedges, s->rows_group, ffp, ffc, st));
+            return RR_OK;
+        };
+        return s->fdbc ? beside(0, tile) : tile();
     } else {
         RR_CK(s->ops->step(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status, s->all,
                            s->block, st));
     }
+    // the staged and the thin-grid steps write the closure's rows: it runs after them
     if (s->fdbc) {
         fc.mode = 0;
         RR_CK(s->ops->fdbc(fc, st));
@@ -507,6 +526,11 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     }
     // the staged step's face rows (rows with y or z on a face, any kind), and
     // its block shape: about 28 KB of populations per stage, two stages
+    if ((rr::staged_ok(*p, s->ops->elem_bytes) || p->face[2] == RR_FACE_FDBC || p->face[3] == RR_FACE_FDBC) &&
+        (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess))
+        return cleanup(fail(RR_ERR_CUDA, "cannot create the side stream"));
     if (rr::staged_ok(*p, s->ops->elem_bytes)) {
         // grouped by the faces a row lies on (z-lo, z-hi, y-lo, y-hi, then the
         // edge rows), so that neighbouring warps run the same compiled face path
@@ -530,10 +554,6 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
             return cleanup(fail(RR_ERR_CUDA, "cannot upload the face-row list"));
         s->nfrows = (uint32_t)frows.size();
         s->bytes += lb;
-        if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming) != cudaSuccess)
-            return cleanup(fail(RR_ERR_CUDA, "cannot create the face-row stream"));
         const size_t row_bytes = (size_t)p->q * p->lx * s->ops->elem_bytes;
         s->stage_rows = (int)std::max<size_t>(
             1, std::min<size_t>({(28672 + row_bytes / 2) / row_bytes, (size_t)p->ly - 2, 32}));
@@ -570,6 +590,9 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         s->les_method = RR_LES_FUSED;
     }
     s->fdbc = (p->face[2] == RR_FACE_FDBC ? 1u : 0u) | (p->face[3] == RR_FACE_FDBC ? 2u : 0u);
+    // the tile step leaves the closure's rows to fdbc_kernel (the staged and
+    // thin-grid steps write them and the closure runs after them)
+    g.fdbc = s->fdbc;
     if (s->fdbc && p->use_les) {
         const size_t slot = 2 * (size_t)p->lx * p->lz;
         if (cudaMalloc(&s->fdbc_wt_mem, 2 * slot * sizeof(double)) != cudaSuccess ||

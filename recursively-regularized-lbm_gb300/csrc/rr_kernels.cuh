@@ -42,6 +42,7 @@ struct Geom {
     uint32_t wallmask;   // bit f: face f is a wall
     int sround;          // FP16/BF16 storage: stochastic (1) or nearest (0) rounding
     int bgk;             // BGK collision with the incompressible velocity (else RR)
+    uint32_t fdbc;       // y rows left to fdbc_kernel by the tile step: bit 0 y = 0, bit 1 y = ny-1
 };
 
 template <typename S> struct CType { using T = float; };
@@ -501,6 +502,8 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
         y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
         fast = false;
     }
+    // the finite-difference closure's wall rows: fdbc_kernel writes them
+    if (!fast && g.fdbc && (((g.fdbc & 1u) && y == 0) || ((g.fdbc & 2u) && y == g.ny - 1))) return;
     const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
     // the force of the streaming half (walls, moments) and of the collision
     T Fx, Fy, Fz, Cx, Cy, Cz;

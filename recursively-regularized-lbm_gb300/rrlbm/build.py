@@ -17,7 +17,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 SOURCES = ["rr_inst_f64.cu", "rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.cu",
            "rr_aux.cu", "rr_api.cu", "rr_batch.cu", "rr_noalloc.cu"]
 HEADERS = ["rr_lattice.cuh", "rr_node.cuh", "rr_node27.cuh", "rr_kernels.cuh", "rr_les.cuh", "rr_dispatch.h",
-           "rr_aux.h", "rr_inst.inc", "rr_internal.h", "rr_stage.cuh"]
+           "rr_aux.h", "rr_inst.inc", "rr_internal.h", "rr_stage.cuh", "rr_fdbc.cuh"]
 
 
 def _stale(target, deps):
