@@ -9,7 +9,8 @@
 // ahead while all threads compute the current block from shared memory (the
 // x shift of a population is an index offset; a periodic x wraps inside the
 // row; a node on an x wall takes its entering populations from its own
-// post-collision values in global memory and applies the closure of that
+// post-collision values, which the producer warp gathers into the stage with
+// plain loads after issuing the copies, and applies the closure of that
 // face), then store their populations straight to global memory.  Rows on a
 // y or z face run in face_kernel, 32 nodes of one row per warp, through the
 // wrap-aware pull and the general face loop.  Each node gets the arithmetic
@@ -115,9 +116,16 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
     const int nx = g.nx;
     const uint32_t NS = a.stages;
     const uint32_t R = a.rows;
+    // x walls: the bounce-back sources of the block's x = 0 and x = nx-1 nodes
+    // (their own post-collision populations), gathered per stage by the
+    // producer warp: wall[s][side][i][r] = f_opp(i) of row r's node on that side
+    const bool xwall = g.face[0] != FACE_PERIODIC;
+    S *wall = buf + (size_t)NS * a.stage_elems;
+    const uint32_t wall_elems = 2u * (uint32_t)LT::Q * R;
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < NS; s++) {
-            mbar_init(&full[s], 1);
+            // the copies' expect_tx arrive, plus the gather's arrive with x walls
+            mbar_init(&full[s], xwall ? 2 : 1);
             mbar_init(&empty[s], STAGE_CONSUMERS / 32);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -126,32 +134,63 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
     // blocks of this CTA: blockIdx.x + k gridDim.x, k = 0 .. mine-1
     const uint32_t mine = blockIdx.x < a.nblocks ? (a.nblocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     if (threadIdx.x >= STAGE_CONSUMERS) {
-        if (threadIdx.x != STAGE_CONSUMERS) return;
-        // the producer
+        // the producer warp: lane 0 waits for the stage and issues the bulk
+        // copies; with x walls every lane then gathers the wall values (else
+        // lane 0 runs alone)
+        const uint32_t lane = threadIdx.x & 31u;
+        if (!xwall && lane != 0) return;
+        const unsigned pmask = xwall ? 0xffffffffu : 1u;
         uint32_t k = 0;
         for (; k < mine; k++) {
             const uint32_t s = k % NS;
-            if (k >= NS && !mbar_wait(&empty[s], (k / NS - 1) & 1u, STAGE_WAIT_LIMIT)) {
+            int ok = 1;
+            if (lane == 0 && k >= NS && !mbar_wait(&empty[s], (k / NS - 1) & 1u, STAGE_WAIT_LIMIT)) {
                 atomicOr(a.status, 4);
-                break;
+                ok = 0;
             }
+            if (!__shfl_sync(pmask, ok, 0)) break;
             int z, y0, rows;
             stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
-            const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
-            S *st = buf + (size_t)s * a.stage_elems;
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(&full[s], (uint32_t)LT::Q * bytes);
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                const size_t src = (size_t)i * g.stride +
-                                   ((size_t)(z - LT::cz(i)) * (size_t)g.ny + (size_t)(y0 - LT::cy(i))) * (size_t)nx;
-                bulk_g2s(st + (size_t)i * R * nx, a.fin + src, bytes, &full[s]);
-            });
+            if (lane == 0) {
+                const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
+                S *st = buf + (size_t)s * a.stage_elems;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(&full[s], (uint32_t)LT::Q * bytes);
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    const size_t src = (size_t)i * g.stride +
+                                       ((size_t)(z - LT::cz(i)) * (size_t)g.ny + (size_t)(y0 - LT::cy(i))) * (size_t)nx;
+                    bulk_g2s(st + (size_t)i * R * nx, a.fin + src, bytes, &full[s]);
+                });
+            }
+            if (xwall) {
+                S *wb = wall + (size_t)s * wall_elems;
+                if ((int)lane < rows) {
+                    const uint32_t row0 = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + (int)lane)) * (uint32_t)nx;
+                    auto gather = [&](auto fc) {
+                        constexpr int F = decltype(fc)::value;
+                        constexpr uint32_t M = entering_mask<LT, F>();
+                        const uint32_t idx = row0 + (F == 0 ? 0u : (uint32_t)nx - 1u);
+                        static_for<LT::Q>([&](auto ic) {
+                            constexpr int i = decltype(ic)::value;
+                            if constexpr (((M >> i) & 1u) != 0)
+                                wb[((size_t)F * LT::Q + i) * R + lane] =
+                                    a.fin[(unsigned long long)LT::opp(i) * g.stride + idx];
+                        });
+                    };
+                    gather(std::integral_constant<int, 0>{});
+                    gather(std::integral_constant<int, 1>{});
+                }
+                // the warp's stores, then one release arrive for all of them
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+            }
         }
         // before the CTA may leave, every copy it issued has landed (the last
         // use of each stage; bounded)
-        for (uint32_t j = (k > NS ? k - NS : 0); j < k; j++)
-            mbar_wait(&full[j % NS], (j / NS) & 1u, STAGE_WAIT_LIMIT);
+        if (lane == 0)
+            for (uint32_t j = (k > NS ? k - NS : 0); j < k; j++)
+                mbar_wait(&full[j % NS], (j / NS) & 1u, STAGE_WAIT_LIMIT);
         return;
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
@@ -163,9 +202,9 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
         int z, y0, rows;
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
+        const S *wb = wall + (size_t)(k % NS) * wall_elems;
         // the main loop takes every node of the block's rows, or with x walls
         // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
-        const bool xwall = g.face[0] != FACE_PERIODIC;
         const int nxi = xwall ? nx - 2 : nx;
         const int nmain = rows * nxi;
         const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
@@ -201,16 +240,16 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
                 });
             } else {
                 // an x wall: the entering populations bounce back from this
-                // node's own post-collision values, then the face's closure
-                auto wall = [&](auto fc) {
+                // node's own post-collision values (gathered into the stage by
+                // the producer), then the face's closure
+                auto wallnode = [&](auto fc) {
                     constexpr int F = decltype(fc)::value;
                     constexpr uint32_t M = entering_mask<LT, F>();
                     const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
                     static_for<LT::Q>([&](auto ic) {
                         constexpr int i = decltype(ic)::value;
                         if constexpr (((M >> i) & 1u) != 0) {
-                            constexpr int o = LT::opp(i);
-                            const T v = ld_dev<T>(a.fin + (unsigned long long)o * g.stride + idx);
+                            const T v = ld_dev<T>(wb + ((size_t)F * LT::Q + i) * R + r);
                             d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
                         } else {
                             d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
@@ -218,8 +257,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
                     });
                     if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
                 };
-                if (x == 0) wall(std::integral_constant<int, 0>{});
-                else wall(std::integral_constant<int, 1>{});
+                if (x == 0) wallnode(std::integral_constant<int, 0>{});
+                else wallnode(std::integral_constant<int, 1>{});
             }
             Mom<T> m = moments<LT>(d);
             T ux, uy, uz;
