@@ -17,7 +17,9 @@ Line fields (one JSON line on rank 0):
              algorithmic bytes = 27 populations x 2 B read + written = 108 B
              per lattice update.
   cpu_baseline  the oracle (C restatement of the reference step, OpenMP on
-             all host threads) on a bounded sample of the same workload.
+             all host threads) on a bounded sample of the same workload;
+             cpu_baseline_1core the same on one thread (the reference's CPU
+             programs are serial).
   batch      the multi-domain form: 256 seeded Taylor-Green / cavity domains
              (FP16 storage) advanced by one persistent launch per step inside
              CUDA graphs, against the same domains stepped one at a time
@@ -175,13 +177,14 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
-def cpu_baseline(wl, budget_s):
-    """the oracle on the machine's host cores, on whole steps of the workload"""
+def cpu_baseline(wl, budget_s, cores=None):
+    """the oracle on the machine's host cores (all of them by default), on whole
+    steps of the workload"""
     from oracle import oracle as O
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from helpers import load_state, oracle_for
     p, st = make(wl)
-    cores = os.cpu_count() or 1
+    cores = cores or os.cpu_count() or 1
     O.set_threads(cores)
     o = oracle_for(p)
     load_state(o, st)
@@ -193,10 +196,12 @@ def cpu_baseline(wl, budget_s):
         el = time.perf_counter() - t0
         if el > budget_s:
             break
+    O.set_threads(os.cpu_count() or 1)
     mlups = p.n * steps / el / 1e6
+    how = f"OpenMP over {cores} threads" if cores > 1 else "one thread"
     return {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
             "sample": f"{steps} full steps of the {p.lx}x{p.ly}x{p.lz} workload in FP64 "
-                      f"({el:.1f} s), OpenMP over {cores} threads"}
+                      f"({el:.1f} s), {how}"}
 
 
 def run_reference(args, rank, world):
@@ -366,6 +371,8 @@ def run_gpu(args, rank, world, local_rank):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
+        # the reference's CPU programs are serial: the like-for-like line
+        line["cpu_baseline_1core"] = cpu_baseline(args.workload, args.cpu_seconds / 2, cores=1)
     if world == 1 and args.batch_steps > 0:
         line["batch"] = run_batch(args)
         line["gpu_launches"] += line["batch"].pop("launches")
