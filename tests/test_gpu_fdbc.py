@@ -246,3 +246,40 @@ def test_fdbc_les_is_two_pass():
         with pytest.raises(rrlbm.RRError) as e:
             s.set_launch(s.launch()[0], les_method=0)
         assert e.value.code == 4
+
+
+@pytest.mark.parametrize("les", [False, True])
+def test_fdbc_d3q19(les):
+    """D3Q19 (Fortran population order) with the FDBC walls."""
+    p, st = presets.channel(nx=20, ny=9, nz=6, Re_tau=15, q=19, les=les, variant="config", amp=0.3)
+    _fdbc(p)
+    o = oracle_for(p)
+    load_state(o, st)
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
+        done = 0
+        for n in (1, 12):
+            s.step(n - done)
+            o.run(n - done)
+            done = n
+            _compare(s, o, st["uc"], n, les)
+
+
+def test_fdbc_les_save_load_restart(tmp_path):
+    """A restart from the reference's files continues the FDBC + WALE run: the
+    wall nodes' tau_t is rebuilt from the saved velocities, as the first
+    collision after the restart takes it."""
+    p, g = _fixture_params(1)
+    o = _loglaw_start(p, 3)
+    with _solver_from(p, o) as s:
+        s.step(9)
+        s.save(str(tmp_path))
+        s.step(6)
+        m1, f1 = s.macro(taut=True), s.get_f()
+    with rrlbm.Solver(p) as s:
+        s.load(str(tmp_path), 9)
+        s.step(6)
+        m2, f2 = s.macro(taut=True), s.get_f()
+    for k in m1:
+        assert np.abs(m1[k] - m2[k]).max() <= 1e-13 * max(1.0, np.abs(m1[k]).max()), k
+    assert np.abs(f1 - f2).max() < 1e-14
