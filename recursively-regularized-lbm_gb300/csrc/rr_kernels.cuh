@@ -362,7 +362,13 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
     });
 }
 
-template <typename S> constexpr int tile_min_blocks() { return sizeof(S) == 8 ? 2 : 5; }
+// resident CTAs per SM the tile step is compiled for (register budget 65536 /
+// (256 x that)): the forced DNS step's collision keeps more values live and
+// runs faster at 4 CTAs with fewer spills (channel 384x192x128 FP16: 352 vs
+// 376 us per step); the WALE passes and the force-free step at 5
+template <typename S, bool F = false, int MODE = 0> constexpr int tile_min_blocks() {
+    return sizeof(S) == 8 ? 2 : ((F && MODE == 0) ? 4 : 5);
+}
 // the batch kernel holds its loop state and the shared descriptor on top of
 // the tile step: one CTA less per SM keeps its spills down
 template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : 4; }
@@ -603,7 +609,7 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
 }
 
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
-__global__ void __launch_bounds__(256, tile_min_blocks<S>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(256, tile_min_blocks<S, FORCE, MODE>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
     tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
 
