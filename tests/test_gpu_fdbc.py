@@ -283,3 +283,22 @@ def test_fdbc_les_save_load_restart(tmp_path):
     for k in m1:
         assert np.abs(m1[k] - m2[k]).max() <= 1e-13 * max(1.0, np.abs(m1[k]).max()), k
     assert np.abs(f1 - f2).max() < 1e-14
+
+
+@pytest.mark.parametrize("les", [False, True])
+def test_fdbc_autotuner_keeps_results(les):
+    """rr_tune's trial launch shapes (tile rows, staged blocks) leave an FDBC
+    solver's populations unchanged, bit for bit."""
+    p, st = presets.channel(nx=32, ny=16, nz=12, Re_tau=27, les=les, storage="f16", variant="config", amp=0.1)
+    _fdbc(p)
+
+    def solver():
+        s = rrlbm.Solver(p)
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
+        return s
+
+    with solver() as s, solver() as r:
+        run = s.tune(trial_steps=2)
+        s.step(3)
+        r.step(run + 3)
+        assert np.array_equal(s.get_f(), r.get_f())
