@@ -53,8 +53,10 @@ struct FdbcArgs {
     uint32_t faces;              // bit 0: y-lo is FDBC, bit 1: y-hi
 };
 
+// 3 CTAs per SM (80 registers): the 384 CTAs of a 384 x 128 channel wall run
+// in one wave beside the tile step
 template <class LT, typename S, bool FORCE, bool FIELD, int MODE>
-__global__ void __launch_bounds__(256) fdbc_kernel(const __grid_constant__ FdbcArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(256, 3) fdbc_kernel(const __grid_constant__ FdbcArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     const int side = (int)blockIdx.z;
     if (!((a.faces >> side) & 1u)) return;
