@@ -99,6 +99,9 @@ rr_status validate(const rr_params *p) {
     if (p->trip_steps < 0) return fail(RR_ERR_INVALID, "trip_steps = %d", p->trip_steps);
     if (p->trip_steps > 0 && (p->q != 27 || p->lx < 3))
         return fail(RR_ERR_UNSUPPORTED, "trip forcing needs D3Q27 and lx >= 3");
+    // forcing_GP scales its field by force_in_x (macrovar.cu:76-115)
+    if (p->trip_steps > 0 && p->force[0] == 0.0)
+        return fail(RR_ERR_UNSUPPORTED, "trip forcing needs a body force along x (force[0] != 0)");
     if (p->collision != RR_COLL_RR && p->collision != RR_COLL_BGK)
         return fail(RR_ERR_INVALID, "collision = %d unknown", p->collision);
     const bool fdbc = p->face[2] == RR_FACE_FDBC || p->face[3] == RR_FACE_FDBC;

@@ -93,6 +93,15 @@ def test_fdbc_unsupported_combinations_rejected(change, msg):
     assert rrlbm.bytes_for(p) == 0
 
 
+def test_trip_forcing_needs_a_force():
+    p, _ = presets.channel(nx=16, ny=12, nz=8, les=False, variant="config")
+    p.trip_steps = 100
+    p.force[0] = 0.0
+    with pytest.raises(rrlbm.RRError) as e:
+        rrlbm.Solver(p)
+    assert e.value.code == 4 and "force" in str(e.value)
+
+
 def test_fdbc_face_kind_range():
     p = _fdbc_channel()
     p.face[2] = p.face[3] = 4
