@@ -192,6 +192,7 @@ cudaError_t readout_state(rr_solver *s, double *fo, double *rho, double *ux, dou
     fc.F = s->p.force;
     fc.status = s->status;
     fc.ffp = ff;
+    fc.ffc = ff; // (no collision in a readout)
     fc.wt = s->fdbc_wt[1 - s->cur];
     fc.fo = fo;
     fc.fo_stride = s->g.n;

@@ -121,14 +121,22 @@ __global__ void __launch_bounds__(256, 3) fdbc_kernel(const __grid_constant__ Fd
     n[3] = -te * gr[0][0];
     n[4] = -te * gr[1][1];
     n[5] = -te * gr[2][2];
+    // the force of the streaming half (closure, moments) and, in the modes
+    // that collide, of the collision
     T Fx, Fy, Fz, Cx, Cy, Cz;
     if constexpr (FIELD) {
         Fx = T(a.ffp[idx]);
         Fy = T(a.ffp[g.stride + idx]);
         Fz = T(a.ffp[2 * g.stride + idx]);
-        Cx = T(a.ffc[idx]);
-        Cy = T(a.ffc[g.stride + idx]);
-        Cz = T(a.ffc[2 * g.stride + idx]);
+        if constexpr (MODE == 0 || MODE == 2) {
+            Cx = T(a.ffc[idx]);
+            Cy = T(a.ffc[g.stride + idx]);
+            Cz = T(a.ffc[2 * g.stride + idx]);
+        } else {
+            Cx = Fx;
+            Cy = Fy;
+            Cz = Fz;
+        }
     } else {
         Fx = Cx = T(a.F[0]);
         Fy = Cy = T(a.F[1]);
