@@ -150,3 +150,25 @@ def test_channel_starts_match_oracle():
     o.init_channel_config(st["uc"], 0.1, 5)
     for k in ("ux", "uy", "uz"):
         assert np.abs(getattr(o, k) - st[k]).max() < 1e-18, k
+
+
+def test_params_layout_matches_the_header(tmp_path):
+    """the ctypes mirror of rr_params has the C struct's size and field offsets"""
+    import ctypes
+    import subprocess
+
+    from conftest import ROOT
+
+    fields = [f[0] for f in rrlbm.Params._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "rr_api.h"\nint main(void) {\n'
+                   '    printf("%zu\\n", sizeof(rr_params));\n' +
+                   "".join(f'    printf("%zu\\n", offsetof(rr_params, {f}));\n' for f in fields) +
+                   "    return 0;\n}\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert out[0] == ctypes.sizeof(rrlbm.Params)
+    assert out[1:] == [getattr(rrlbm.Params, f).offset for f in fields]
