@@ -60,3 +60,20 @@ def test_channel_config_profile_f16():
     err = np.abs(u16 - u64).max() / uc
     print(f"\nWALE channel 384x192x128 2000 steps f16: max |<u>16 - <u>64| / U_c = {err:.2e}")
     assert err < 1e-2
+
+
+def test_cavity_reference_probe_100k():
+    """The Cavity program's own check (Cavity/33contour1000.ipynb cell 2): the
+    128 x 128 x 2 cavity at Re = 1000 (lid at x = lx moving +y, 0.1) after
+    100,000 steps, u_x / u_w averaged over the two mid-x nodes of the last y
+    row; the notebook prints -0.022819644872579658 from the program's FP64
+    output ux100000.dat.  Measured: -0.022819644872338 (2.4e-13 from it);
+    bar 1e-11."""
+    p, st = presets.cavity(n=128, Re=1000.0, U=0.1, variant="reference")
+    with rrlbm.Solver(p) as s:
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"])
+        s.step(100000)
+        m = s.macro()
+    probe = 0.5 * (m["ux"][0, 127, 63] + m["ux"][0, 127, 64]) / 0.1
+    print(f"\ncavity 128x128x2 Re 1000, step 100000: probe {probe:.15f} (reference -0.022819644872579658)")
+    assert abs(probe - (-0.022819644872579658)) < 1e-11
