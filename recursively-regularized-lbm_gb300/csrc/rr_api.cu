@@ -334,10 +334,13 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         RR_CK(cudaEventRecord(s->fork, st));
         RR_CK(cudaStreamWaitEvent(s->side, s->fork, 0));
         RR_CK(s->ops->fdbc(fc, s->side));
-        rr_status r = main();
+        const rr_status r = main();
+        // join the side stream whether or not the main launch went in (a
+        // capture must not end with the fork open)
+        cudaError_t e = cudaEventRecord(s->join, s->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->join, 0);
         if (r != RR_OK) return r;
-        RR_CK(cudaEventRecord(s->join, s->side));
-        RR_CK(cudaStreamWaitEvent(st, s->join, 0));
+        if (e != cudaSuccess) return fail(RR_ERR_CUDA, "side-stream join failed: %s", cudaGetErrorString(e));
         return RR_OK;
     };
     if (s->p.use_les) {
