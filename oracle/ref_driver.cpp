@@ -181,6 +181,31 @@ void ref_run_fdbc(int nsteps, double *f, double *f_temp, double *rho, double *ux
     for (int i = 0; i < nsteps; i++) ref_step_fdbc(f, f_temp, rho, ux, uy, uz, fx, fy, fz, taut);
 }
 
+/* ref_run_trip with FDBC in place of RRBC, run as in ref_step_fdbc */
+void ref_run_trip_fdbc(int nsteps, long long start_istep, int npforcing, double *f, double *f_temp, double *rho,
+                       double *ux, double *uy, double *uz, double *fx, double *fy, double *fz, double *taut) {
+    srand(12345);
+    for (long long n = start_istep + 1; n <= start_istep + nsteps; n++) {
+        if (n < npforcing) {
+            d_istep = (int)n;
+            if (n % 2000 == 0) d_rand_phase = (double)rand() / RAND_MAX;
+            launch([&] { forcing_GP(fx, fy, fz); });
+        } else {
+            launch([&] { forcing(fx, fy, fz); });
+        }
+        d_istep = 1; /* collision_RR prints every 1000 steps otherwise */
+        if (USE_LES) launch([&] { LES_WALE(ux, uy, uz, taut); });
+        launch([&] { collision_RR(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+        launch([&] { streaming(f, f_temp); });
+        launch([&] { BB(f, f_temp); });
+        memcpy(f, f_temp, sizeof(double) * (size_t)NPOP * LXYZ);
+        launch([&] { macrovar(f, fx, fy, fz, rho, ux, uy, uz); });
+        launch_serial([&] { FDBC(f_temp, fx, fy, fz, rho, ux, uy, uz, taut); });
+        launch_serial([&] { FDBC(f, fx, fy, fz, rho, ux, uy, uz, taut); });
+        launch([&] { macrovar_BN(f, fx, fy, fz, rho, ux, uy, uz); });
+    }
+}
+
 /* rand() of this C library after srand(seed), n values (checks of the restatement) */
 void ref_rand(unsigned seed, int n, int *out) {
     srand(seed);

@@ -239,6 +239,30 @@ def test_trip_forcing_matches_reference_live(les):
         assert np.array_equal(getattr(s, k), a), k
 
 
+@pytest.mark.parametrize("les", [0, 1])
+def test_fdbc_trip_forcing_matches_reference_live(les):
+    """FDBC walls with the start-up trip forcing (per-node force fields read
+    by the closure), bit for bit against the reference's kernels, across the
+    phase draw at step 2000 and the switch to the uniform force."""
+    R = _ref_lib(les)
+    R.ref_run_trip_fdbc.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_int] + [ctypes.c_void_p] * 10
+    npforcing, steps = 2050, 2100
+    s = O.Sim(16, 12, 8, q=27, order=O.ORDER_CUDA, cs_mode=O.CS_SQRT_RT, tau=R.ref_tau(),
+              force=(R.ref_force_in_x(), 0.0, 0.0), les=bool(les), cw=0.5,
+              faces=(0, 0, O.FACE_FDBC, O.FACE_FDBC, 0, 0))
+    s.init_channel_loglaw(R.ref_ustar(), R.ref_ystar())
+    s.enable_trip(npforcing)
+    f, rho, ux, uy, uz = (a.copy() for a in (s.f, s.rho, s.ux, s.uy, s.uz))
+    ft, fx, fy, fz, taut = (np.zeros_like(a) for a in (f, rho, rho, rho, rho))
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    R.ref_run_trip_fdbc(steps, 0, npforcing, P(f), P(ft), P(rho), P(ux), P(uy), P(uz), P(fx), P(fy), P(fz),
+                        P(taut))
+    s.run(steps)
+    assert np.array_equal(s.f, f)
+    for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
+        assert np.array_equal(getattr(s, k), a), k
+
+
 def test_bgk_matches_reference_live():
     """The oracle's BGK collision (BGK/collision.cu) and incompressible
     moments (BGK/macrovar.cu) with half-way bounce-back at y walls against the
