@@ -134,6 +134,7 @@ void ref_run(int nsteps, double *f, double *f_temp, double *rho, double *ux, dou
 void ref_run_trip(int nsteps, long long start_istep, int npforcing, double *f, double *f_temp, double *rho,
                   double *ux, double *uy, double *uz, double *fx, double *fy, double *fz, double *taut) {
     srand(12345);
+    d_rand_phase = 0.0; /* as at the start of a run (globals.cu), whatever an earlier call left */
     for (long long n = start_istep + 1; n <= start_istep + nsteps; n++) {
         if (n < npforcing) {
             d_istep = (int)n;
@@ -185,6 +186,7 @@ void ref_run_fdbc(int nsteps, double *f, double *f_temp, double *rho, double *ux
 void ref_run_trip_fdbc(int nsteps, long long start_istep, int npforcing, double *f, double *f_temp, double *rho,
                        double *ux, double *uy, double *uz, double *fx, double *fy, double *fz, double *taut) {
     srand(12345);
+    d_rand_phase = 0.0; /* as at the start of a run (globals.cu), whatever an earlier call left */
     for (long long n = start_istep + 1; n <= start_istep + nsteps; n++) {
         if (n < npforcing) {
             d_istep = (int)n;
