@@ -85,20 +85,28 @@ def make(wl):
     return presets.taylor_green(L=100, nz=4, tau=0.6, Ma=0.01, storage=w["storage"])
 
 
-def describe(wl, p, storage):
+def describe(wl, p):
+    """the workload, the same string on both arms (the storage type is the
+    line's dtype)"""
     kind = WORKLOADS[wl]["kind"]
     if kind == "cavity":
         return (f"lid-driven cavity {p.lx}x{p.ly}x{p.lz} D3Q27 RR, Re=1000, lid 0.1 +x on y-hi, "
-                f"bounce-back + regularized closure on 6 faces, {storage} storage")
+                f"bounce-back + regularized closure on 6 faces")
     if kind == "channel":
         w = WORKLOADS[wl]
         model = "RR + WALE (C_w=0.5)" if w.get("les", True) else "RR DNS"
         walls = "finite-difference closure (FDBC)" if w.get("fdbc") else "bounce-back + regularized closure"
         return (f"channel {p.lx}x{p.ly}x{p.lz} D3Q27 {model}, Re_tau=180, walls y ({walls}), periodic x/z, "
-                f"body force, {storage} storage")
+                f"body force")
     ma = 0.05 if kind == "tg128" else 0.01
     coll = "BGK" if WORKLOADS[wl].get("bgk") else "RR"
-    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 {coll}, Ma={ma}, tau=0.6, periodic, {storage} storage"
+    return f"Taylor-Green {p.lx}x{p.ly}x{p.lz} D3Q27 {coll}, Ma={ma}, tau=0.6, periodic"
+
+
+def config_of(wl, p, world):
+    """the line's config, identical on the GPU arm and the reference arm"""
+    return {"workload": describe(wl, p), "nodes": p.n, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: flushed (256 MB write) before every timed step; the CPU arm has no flush"}
 
 
 def peaks():
@@ -229,8 +237,7 @@ def run_reference(args, rank, world):
             "impl": "reference", "n_gpus": args.gpus, "steps": K, "warmup": W,
             "ms_per_step": el / Ks * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": describe(args.workload, p, "f64") + " (oracle: C restatement of the "
-                                   "reference step, FP64)"},
+            "config": config_of(args.workload, p, world),
             "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
                              "sample": f"{Ks} of the {K} requested full steps (at most ~2 min of host work) after "
                                        f"{max(W, 1)} warm-up steps, OpenMP over {cores} threads"},
@@ -356,9 +363,7 @@ def run_gpu(args, rank, world, local_rank):
         "metric": "D3Q27 RR MLUPS (lattice updates per second)", "value": value, "unit": "MLUPS",
         "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": t_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": DTYPE[storage], "data": "synthetic",
-        "config": {"workload": describe(args.workload, p, storage),
-                   "nodes": n, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed (256 MB write) before every timed step"},
+        "config": config_of(args.workload, p, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "bytes_per_lup": bpl, "peak_source": f"{src} (hbm_gbs)"},

@@ -39,7 +39,8 @@ typedef enum {
     RR_ERR_CUDA = 2,        /* a CUDA runtime call failed */
     RR_ERR_NOMEM = 3,       /* device or host allocation failed */
     RR_ERR_UNSUPPORTED = 4, /* combination not built */
-    RR_ERR_WATCHDOG = 5,    /* density left (0.1, 10) or became NaN */
+    RR_ERR_WATCHDOG = 5,    /* density left (0.1, 10) or became NaN, or a bounded
+                               wait of the staged step gave up (rr_last_error says which) */
     RR_ERR_IO = 6,          /* file could not be opened / read / written */
     RR_ERR_STATE = 7        /* call out of order (e.g. step before init) */
 } rr_status;
@@ -172,7 +173,10 @@ rr_status rr_diag(rr_solver *s, double out[4]);
  * 2147483647.  The first call on a device looks up that array's device
  * address (with the device current), so make it before any stream capture.
  * Calls share the array: two calls that overlap on the GPU race.  Nothing is
- * synchronised; read out[] after the stream's work completes. */
+ * synchronised; read out[] after the stream's work completes.  The looked-up
+ * address is kept for the life of the process: after a cudaDeviceReset() of a
+ * device the library's device memory there is gone, so do not call this
+ * function on that device again in the same process. */
 rr_status rr_diag_fields_noalloc(const double *rho, const double *ux, const double *uy,
                                  const double *uz, size_t n, double *out, void *stream);
 
@@ -296,6 +300,17 @@ rr_status rr_batch_tune(rr_batch *b, int trial_steps, long long *steps_run);
 typedef enum { RR_DNS_TILE = 0, RR_DNS_STAGED = 1 } rr_dns_method;
 rr_status rr_set_stage(rr_solver *s, int method, int rows, int stages);
 rr_status rr_get_stage(const rr_solver *s, int *method, int *rows, int *stages);
+/* Every wait of the staged step's copy pipeline (an mbarrier poll loop) is
+ * bounded: after `polls` unsuccessful polls the waiting warp records
+ * RR_ERR_WATCHDOG (reported by the next rr_sync, "a wait of the staged step's
+ * pipeline timed out"), its CTA stops, and the CTA's copy-issuing thread waits
+ * for the copies it has in flight before it exits.  polls < 0 restores the
+ * default (2^24); 0 makes every wait give up at once, so the timeout path can
+ * be exercised.  The state of a step whose wait gave up is not valid: set it
+ * again (rr_init_state / rr_load).  No counterpart in the reference, whose
+ * kernels do not wait on one another. */
+rr_status rr_set_wait_limit(rr_solver *s, long long polls);
+long long rr_get_wait_limit(const rr_solver *s);
 
 #ifdef __cplusplus
 }

@@ -333,12 +333,14 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
         fc.mode = mode;
         RR_CK(cudaEventRecord(s->fork, st));
         RR_CK(cudaStreamWaitEvent(s->side, s->fork, 0));
-        RR_CK(s->ops->fdbc(fc, s->side));
-        const rr_status r = main();
-        // join the side stream whether or not the main launch went in (a
-        // capture must not end with the fork open)
+        // once the side stream is forked, every path joins it again before
+        // returning (a capture must not end with the fork open)
+        const cudaError_t ef = s->ops->fdbc(fc, s->side);
+        const rr_status r = ef == cudaSuccess ? main() : RR_OK;
         cudaError_t e = cudaEventRecord(s->join, s->side);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, s->join, 0);
+        if (ef != cudaSuccess)
+            return fail(RR_ERR_CUDA, "finite-difference closure launch failed: %s", cudaGetErrorString(ef));
         if (r != RR_OK) return r;
         if (e != cudaSuccess) return fail(RR_ERR_CUDA, "side-stream join failed: %s", cudaGetErrorString(e));
         return RR_OK;
@@ -364,7 +366,8 @@ rr_status launch_one(rr_solver *s, const void *fin, void *fout, cudaStream_t st,
                                    s->tile, st));
     } else if (s->p.lx >= 3 && s->dns_method == RR_DNS_STAGED && s->frow_list && !ffp && !s->g.bgk) {
         RR_CK(s->ops->staged(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
-                             s->frow_list, s->nfrows, s->stage_rows, s->stages, st, s->side, s->fork, s->join));
+                             s->frow_list, s->nfrows, s->stage_rows, s->stages, s->stage_wait, st, s->side, s->fork,
+                             s->join));
     } else if (s->p.lx >= 3) {
         auto tile = [&]() -> rr_status {
             RR_CK(s->ops->tile(s->p.q, force, fin, fout, s->g, 1.0 - 1.0 / s->p.tau, s->p.force, s->status,
@@ -771,9 +774,26 @@ rr_status rr_sync(rr_solver *s) {
     int flag = 0;
     RR_CK(cudaMemcpyAsync(&flag, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     RR_CK(cudaStreamSynchronize(s->stream));
-    if (flag) return fail(RR_ERR_WATCHDOG, "density left (0.1, 10) or became NaN by step %lld", s->istep);
+    if (flag & rr::WATCH_STAGE_WAIT)
+        return fail(RR_ERR_WATCHDOG, "watchdog %d: a wait of the staged step's pipeline timed out by step %lld",
+                    flag, s->istep);
+    if (flag) return fail(RR_ERR_WATCHDOG, "watchdog %d: density left (0.1, 10) or became NaN by step %lld", flag,
+                          s->istep);
     return RR_OK;
 }
+
+rr_status rr_set_wait_limit(rr_solver *s, long long polls) {
+    if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
+    if (polls > 0xFFFFFFFFll) return fail(RR_ERR_INVALID, "polls = %lld exceeds 2^32-1", polls);
+    const uint32_t v = polls < 0 ? rr::STAGE_WAIT_LIMIT : (uint32_t)polls;
+    if (v != s->stage_wait) {
+        s->stage_wait = v;
+        rr::drop_graph(s); // the captured steps carry the old limit
+    }
+    return RR_OK;
+}
+
+long long rr_get_wait_limit(const rr_solver *s) { return s ? (long long)s->stage_wait : -1; }
 
 long long rr_get_istep(const rr_solver *s) { return s ? s->istep : -1; }
 

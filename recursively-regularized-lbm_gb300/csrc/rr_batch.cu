@@ -496,8 +496,10 @@ rr_status rr_batch_sync(rr_batch *b) {
     for (int k = 0; k < n; k++)
         if (b->status_host[k])
             return rr_internal_error(RR_ERR_WATCHDOG,
-                                     "watchdog: density out of range or NaN in batch member %d (step <= %lld)", k,
-                                     b->members[k]->istep);
+                                     (b->status_host[k] & rr::WATCH_STAGE_WAIT)
+                                         ? "watchdog %d: a pipeline wait timed out in batch member %d (step <= %lld)"
+                                         : "watchdog %d: density out of range or NaN in batch member %d (step <= %lld)",
+                                     b->status_host[k], k, b->members[k]->istep);
     return RR_OK;
 }
 

@@ -13,6 +13,14 @@ namespace rr {
 
 struct Geom;
 
+// polls of an mbarrier before a wait of the staged step gives up (its
+// default; rr_set_wait_limit changes the run-time limit of a solver)
+constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 24;
+
+// bits of a solver's device watchdog word
+constexpr int WATCH_DENSITY = 1; // density left (0.1, 10) or became NaN
+constexpr int WATCH_STAGE_WAIT = 4; // a wait of the staged step's pipeline gave up
+
 struct LesTile {
     int tx, ty, zchunk; // tile of the WALE step kernel (autotuned per size class)
 };
@@ -64,10 +72,13 @@ struct Ops {
     // y/z face (frows) in one launch, the interior rows in blocks of R rows
     // through an NS-stage shared-memory pipeline of bulk copies
     // (side, fork, join: a second stream and two events for the face-row
-    // launch; side == NULL runs both launches on st)
+    // launch; side == NULL runs both launches on st); wait_limit: polls
+    // before a pipeline wait gives up (the drain before a CTA exits always
+    // takes STAGE_WAIT_LIMIT)
     cudaError_t (*staged)(int q, bool force, const void *fin, void *fout, const Geom &g, double om1,
                           const double F[3], int *status, const uint32_t *frows, uint32_t nfrows, int R, int NS,
-                          cudaStream_t st, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
+                          uint32_t wait_limit, cudaStream_t st, cudaStream_t side, cudaEvent_t fork,
+                          cudaEvent_t join);
     // the tile step's descriptor of one domain (TileArgs, written to out when
     // out != NULL) for a batch launch; returns its size, *nitems its warp items
     size_t (*tile_desc)(int q, const void *fin, void *fout, const Geom &g, double om1, const double F[3],

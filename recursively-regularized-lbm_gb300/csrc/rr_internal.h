@@ -70,6 +70,7 @@ struct rr_solver {
     int rows_group = 32; // tile step: rows per work-item group (autotuned)
     int dns_method = RR_DNS_TILE; // DNS step: tile step or staged step
     int stage_rows = 2, stages = 3; // staged step: rows per block, pipeline stages
+    uint32_t stage_wait = rr::STAGE_WAIT_LIMIT; // staged step: polls before a pipeline wait gives up
     uint32_t *frow_list = nullptr;  // staged step: rows on a y or z face
     uint32_t nfrows = 0;
     cudaStream_t side = nullptr;     // staged step: the face-row launch, beside the interior one

@@ -16,11 +16,14 @@
 // wrap-aware pull and the general face loop.  Each node gets the arithmetic
 // of the tile step, so the results are the same bit for bit.
 //
-// Every mbarrier wait is bounded: a wait that gives up sets bit 2 of the
-// watchdog word, the CTA stops taking blocks and its issuing thread waits
-// (bounded again) for the copies it still has in flight before it exits.
+// Every mbarrier wait is bounded: a wait that gives up (after
+// StageArgs::wait_limit polls) sets WATCH_STAGE_WAIT in the watchdog word, the
+// CTA stops taking blocks and its issuing thread waits (bounded again, always
+// STAGE_WAIT_LIMIT polls) for the copies it still has in flight before it
+// exits, so that no bulk copy lands in the shared memory of an exited CTA.
 #pragma once
 
+#include "rr_dispatch.h"
 #include "rr_kernels.cuh"
 
 namespace rr {
@@ -41,6 +44,7 @@ struct StageArgs {
     double om1;
     double F[3];
     int *status;
+    uint32_t wait_limit;  // polls before a pipeline wait gives up (the final drain: STAGE_WAIT_LIMIT)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -85,8 +89,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
-
-constexpr uint32_t STAGE_WAIT_LIMIT = 1u << 24; // polls before a wait gives up
 
 // first row and row count of block b
 __device__ __forceinline__ void stage_block(uint32_t b, const FastDiv &div_yblocks, uint32_t yblocks, uint32_t R,
@@ -144,8 +146,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
         for (; k < mine; k++) {
             const uint32_t s = k % NS;
             int ok = 1;
-            if (lane == 0 && k >= NS && !mbar_wait(&empty[s], (k / NS - 1) & 1u, STAGE_WAIT_LIMIT)) {
-                atomicOr(a.status, 4);
+            if (lane == 0 && k >= NS && !mbar_wait(&empty[s], (k / NS - 1) & 1u, a.wait_limit)) {
+                atomicOr(a.status, WATCH_STAGE_WAIT);
                 ok = 0;
             }
             if (!__shfl_sync(pmask, ok, 0)) break;
@@ -195,8 +197,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
     for (uint32_t k = 0; k < mine; k++) {
-        if (!mbar_wait(&full[k % NS], (k / NS) & 1u, STAGE_WAIT_LIMIT)) {
-            if ((threadIdx.x & 31u) == 0) atomicOr(a.status, 4);
+        if (!mbar_wait(&full[k % NS], (k / NS) & 1u, a.wait_limit)) {
+            if ((threadIdx.x & 31u) == 0) atomicOr(a.status, WATCH_STAGE_WAIT);
             break;
         }
         int z, y0, rows;

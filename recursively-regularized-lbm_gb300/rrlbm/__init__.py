@@ -106,6 +106,8 @@ def lib():
             "rr_get_stage": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                               ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_batch_tune": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)], ctypes.c_int),
+            "rr_set_wait_limit": ([vp, ctypes.c_longlong], ctypes.c_int),
+            "rr_get_wait_limit": ([vp], ctypes.c_longlong),
             "rr_get_launch": ([vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_set_launch": ([vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
@@ -128,6 +130,32 @@ def params_default():
     """parameters.h + globals.cu defaults (64^3 Re_tau=180 channel, DNS, FP64)."""
     p = Params()
     _check(lib().rr_params_default(ctypes.byref(p)))
+    return p
+
+
+def params_host_default():
+    """The same defaults as rr_params_default, filled in on the host without
+    loading the CUDA library (the presets use it, so that CPU-only callers
+    of the workload definitions never map librrlbm.so): parameters.h:9-11
+    (64^3) and globals.cu:33-38 (Re_tau = 180, nu = 0.000622,
+    u* = 2 Re_tau nu / LY, tau = 3 nu + 0.5, F_x = 2 u*^2 / LY), walls at
+    y = 0 and y = LY-1, D3Q27, FP64, CUDA order, stochastic rounding."""
+    p = Params()
+    p.lx = p.ly = p.lz = 64
+    p.q = 27
+    p.use_les = 0
+    Re, visc = 180.0, 0.000622
+    u0 = 2.0 * Re * visc / p.ly
+    p.tau = 3.0 * visc + 0.5
+    p.cw = 0.5
+    p.force[0] = 2.0 * u0 * u0 / p.ly
+    p.face[2] = p.face[3] = FACE_WALL
+    p.storage = STORE_F64
+    p.order = ORDER_CUDA
+    p.device = 0
+    p.ustar = u0
+    p.ystar = visc / u0
+    p.rounding = ROUND_STOCHASTIC
     return p
 
 
@@ -286,6 +314,14 @@ class Solver:
     def set_stage(self, method, rows=None, stages=None):
         _, r, n = self.stage()
         _check(lib().rr_set_stage(self._h, int(method), int(rows or r), int(stages or n)))
+
+    def set_wait_limit(self, polls):
+        """polls before a wait of the staged step's pipeline gives up (< 0: the default)"""
+        _check(lib().rr_set_wait_limit(self._h, int(polls)))
+
+    @property
+    def wait_limit(self):
+        return lib().rr_get_wait_limit(self._h)
 
     def set_launch(self, rows_group, les_method=None, les_tile=None):
         m = None if les_method is None else ctypes.byref(ctypes.c_int(int(les_method)))

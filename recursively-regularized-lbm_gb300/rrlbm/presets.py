@@ -12,7 +12,8 @@ import math
 
 import numpy as np
 
-from . import (FACE_PERIODIC, FACE_WALL, ORDER_CUDA, ORDER_FORTRAN, STORAGE, params_default)
+from . import (FACE_PERIODIC, FACE_WALL, ORDER_CUDA, ORDER_FORTRAN, STORAGE)
+from . import params_host_default as params_default
 
 # D3Q27 in the CUDA order (initial.cu:67-69), D3Q19 in the Fortran order
 # (Taylor_Green/D3Q19RR.f90:75-77); the solver's internal orders

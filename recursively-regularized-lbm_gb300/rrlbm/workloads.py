@@ -17,7 +17,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import FACE_PERIODIC, FACE_WALL, ORDER_CUDA, STORAGE, params_default
+from . import FACE_PERIODIC, FACE_WALL, ORDER_CUDA, STORAGE
+from . import params_host_default as params_default
 
 CS = 1.0 / math.sqrt(3.0)
 CHANNEL_USTAR = 0.0025  # friction velocity of served channels (centreline ~0.06)

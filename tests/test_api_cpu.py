@@ -38,6 +38,12 @@ def test_defaults_follow_parameters_h():
     assert list(p.face) == [0, 0, 1, 1, 0, 0]
 
 
+def test_host_defaults_equal_the_library_defaults():
+    """the presets' host-side defaults are rr_params_default byte for byte"""
+    a, b = rrlbm.params_default(), rrlbm.params_host_default()
+    assert bytes(a) == bytes(b)
+
+
 @pytest.mark.parametrize("field,value,msg", [
     ("q", 15, "q = 15"), ("tau", 0.5, "tau"), ("lx", 0, "grid"), ("storage", 9, "storage"),
 ])

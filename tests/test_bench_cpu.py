@@ -62,3 +62,28 @@ def test_reference_arm_two_ranks():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert "workload" in d["config"]
+
+
+def test_reference_arm_maps_no_cuda_library():
+    """the reference arm (the oracle on the host cores) builds its workload
+    without loading the product's CUDA library, and prints the same config
+    as the GPU arm"""
+    code = (
+        "import json, sys, types\n"
+        "sys.argv = ['bench.py']\n"
+        "import bench\n"
+        "args = types.SimpleNamespace(steps=1, warmup=1, gpus=1, workload='tg100_f64')\n"
+        "bench.run_reference(args, 0, 1)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('MAPPED' if 'librrlbm' in maps else 'CLEAN')\n"
+        "p, st = bench.make('tg100_f64')\n"
+        "print(json.dumps(bench.config_of('tg100_f64', p, 1)))\n")
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT,
+                       env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = r.stdout.splitlines()
+    assert "CLEAN" in out, r.stdout
+    line = json.loads([l for l in out if l.startswith('{"metric"')][0])
+    assert line["config"] == json.loads(out[-1])
+    assert "f64" not in line["config"]["workload"] and line["dtype"] == "f64"

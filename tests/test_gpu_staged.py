@@ -73,3 +73,34 @@ def test_staged_rejections():
             s.set_stage(1, 22, 4)  # 4 stages x 22 rows x 24 x 27 x 8 B > 227 KB
         with pytest.raises(rrlbm.RRError):
             s.set_stage(1, 1, 5)
+
+
+@pytest.mark.parametrize("k", [4, 0])  # periodic box; six-wall cavity (the x-wall gather path)
+def test_staged_wait_timeout_reports_and_recovers(k):
+    """Every pipeline wait of the staged step is bounded.  With a limit of 0
+    polls every wait gives up at once: the step returns (no hang), rr_sync
+    reports the pipeline timeout, and after the default limit is restored and
+    the state set again the solver steps exactly as the tile step does."""
+    p, st = _cases()[k]
+    with rrlbm.Solver(p) as s:
+        s.set_stage(1, 2, 2)
+        assert s.wait_limit == 1 << 24
+        s.set_wait_limit(0)
+        assert s.wait_limit == 0
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
+        s.step(3)
+        with pytest.raises(rrlbm.RRError) as e:
+            s.sync()
+        assert e.value.code == 5 and "pipeline timed out" in str(e.value)
+        s.set_wait_limit(-1)
+        assert s.wait_limit == 1 << 24
+        s.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
+        s.step(70)
+        s.sync()
+        got = s.get_f()
+    with rrlbm.Solver(p) as t:
+        t.set_stage(0)
+        t.init_state(st["rho"], st["ux"], st["uy"], st["uz"], f=st.get("f"))
+        t.step(70)
+        want = t.get_f()
+    assert np.array_equal(got, want)
