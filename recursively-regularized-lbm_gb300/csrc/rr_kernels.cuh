@@ -26,6 +26,7 @@
 #include <cuda_fp16.h>
 
 #include "rr_node.cuh"
+#include "rr_pair.cuh"
 
 namespace rr {
 
@@ -275,6 +276,7 @@ struct TileArgs {
     const S *fin;
     Geom g;
     uint32_t nitems, nrows, segs, group_items;
+    uint32_t pairs;                  // row items take 64 nodes, two x-adjacent nodes per lane (packed FP32 pairs)
     uint32_t rows_group, xf_half;    // rows per group; x-face items per face per group
     uint32_t nmain;                  // items of the row groups; the rest are edge items
     const uint32_t *edges;           // x-end nodes of rows on a y/z wall face
@@ -363,15 +365,19 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 }
 
 // resident CTAs per SM the tile step is compiled for (register budget 65536 /
-// (256 x that)): the forced DNS step's collision keeps more values live and
-// runs faster at 4 CTAs with fewer spills (channel 384x192x128 FP16: 352 vs
-// 376 us per step); the WALE passes and the force-free step at 5
-template <typename S, bool F = false, int MODE = 0> constexpr int tile_min_blocks() {
-    return sizeof(S) == 8 ? 2 : ((F && MODE == 0) ? 4 : 5);
+// (256 x that)).  The DNS step of 16- and 32-bit storage carries the packed
+// pair path (two nodes' populations live per thread): 2 CTAs, 128 registers.
+// The WALE passes and the BGK step run one node per thread at 5, the
+// trip-forcing step (per-node force fields) at 4.
+#ifndef RR_PAIR_MIN_BLOCKS
+#define RR_PAIR_MIN_BLOCKS 2
+#endif
+template <typename S, int MODE = 0, bool FIELD = false, bool BGK = false> constexpr int tile_min_blocks() {
+    return sizeof(S) == 8 ? 2 : (MODE != 0 ? 5 : FIELD ? 4 : BGK ? 5 : RR_PAIR_MIN_BLOCKS);
 }
 // the batch kernel holds its loop state and the shared descriptor on top of
-// the tile step: one CTA less per SM keeps its spills down
-template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : 4; }
+// the tile step's registers
+template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : RR_PAIR_MIN_BLOCKS; }
 
 template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
 template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
@@ -451,63 +457,12 @@ __host__ __device__ __forceinline__ void collide_bgk(T (&d)[LT::Q], T drho, T ux
     });
 }
 
-// one work item (one warp) of the tile step; A is TileArgs wherever it lives
-// (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
-// DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
-// applies the walls and writes the velocity field; MODE 2 streams again,
-// takes tau_t from the 7-point stencil of that field and collides.
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
-__device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
+// one node of the tile step (row, x, y, z); fast: a row off every y/z face and
+// x in [1, nx-2] (no wrap, no wall: the precomputed upstream addresses)
+template <class LT, typename S, bool FORCE, int MODE, bool FIELD, bool BGK, class A>
+__device__ __forceinline__ void tile_node(const A &a, uint32_t row, int x, int y, int z, bool fast) {
     using T = typename CType<S>::T;
-    if (item >= a.nitems) return;
     const Geom &g = a.g;
-    uint32_t row;
-    int x, y, z;
-    bool fast;
-    // the slow items go first so that they overlap the bulk instead of
-    // forming a tail: the edge items, then the rows of the last z plane (the
-    // row order is rotated by one plane)
-    const uint32_t nedge_items = a.nitems - a.nmain;
-    if (item >= nedge_items) {
-        const uint32_t mitem = item - nedge_items;
-        const uint32_t grp = fdiv(mitem, a.div_group);
-        const uint32_t sub = mitem - grp * a.group_items;
-        bool xface = false;
-        if (sub < a.rows_group * a.segs) {
-            const uint32_t rl = fdiv(sub, a.div_segs);
-            row = grp * a.rows_group + rl;
-            x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
-            fast = true;
-            if (x > g.nx - 2) return;
-        } else {
-            // the x = 0 nodes of the group's rows, 32 per item, then the
-            // x = nx-1 nodes: whole CTAs of these slower items
-            const uint32_t xi = sub - a.rows_group * a.segs;
-            const bool lo = xi < a.xf_half;
-            row = grp * a.rows_group + (lo ? xi : xi - a.xf_half) * 32u + lane;
-            x = lo ? 0 : g.nx - 1;
-            fast = false;
-            xface = true;
-        }
-        if (row >= a.nrows) return;
-        row += a.rot;
-        if (row >= a.nrows) row -= a.nrows;
-        z = (int)fdiv(row, a.div_ny);
-        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
-        const bool yzw = ((a.yzwall & 1u) && y == 0) || ((a.yzwall & 2u) && y == g.ny - 1) ||
-                         ((a.yzwall & 4u) && z == 0) || ((a.yzwall & 8u) && z == g.nz - 1);
-        if (xface && yzw) return; // an edge node: handled by the edge items
-        fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
-    } else {
-        const uint32_t e = item * 32u + lane;
-        if (e >= a.nedges) return;
-        const uint32_t nidx = a.edges[e];
-        row = fdiv(nidx, a.div_nx);
-        x = (int)(nidx - row * (uint32_t)g.nx);
-        z = (int)fdiv(row, a.div_ny);
-        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
-        fast = false;
-    }
     // the finite-difference closure's wall rows: fdbc_kernel writes them
     if (!fast && g.fdbc && (((g.fdbc & 1u) && y == 0) || ((g.fdbc & 2u) && y == g.ny - 1))) return;
     const uint32_t idx = row * (uint32_t)g.nx + (uint32_t)x;
@@ -608,8 +563,148 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     });
 }
 
+// Stores two x-adjacent nodes' populations (idx: the first node, at an odd
+// element offset, so every store is a 16- or 32-bit scalar store).  With
+// stochastic rounding each node draws from its own stream exactly as
+// store_sr_pairs does for a node alone: per population pair (i0, i1) one LCG
+// draw r, folded f = r ^ (r >> 16), whose low half rounds i0 and high half
+// i1; one packed conversion rounds population i of both nodes, the first
+// node's bits in the low half of the random operand, the second's in the high.
+template <class LT, typename S>
+__device__ __forceinline__ void store_pair(S *const *dst, uint32_t idx, const F2 (&d)[LT::Q], bool sround,
+                                           uint32_t sa, uint32_t sb) {
+    if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+        if (sround) {
+            uint32_t ra = sa, rb = sb;
+            auto put = [&](S *p, uint32_t w) {
+                *reinterpret_cast<unsigned short *>(p) = (unsigned short)(w & 0xFFFFu);
+                *reinterpret_cast<unsigned short *>(p + 1) = (unsigned short)(w >> 16);
+            };
+            static_for<(LT::Q + 1) / 2>([&](auto jc) {
+                constexpr int i0 = 2 * decltype(jc)::value, i1 = i0 + 1;
+                ra = ra * 1664525u + 1013904223u;
+                rb = rb * 1664525u + 1013904223u;
+                const uint32_t fa = ra ^ (ra >> 16), fb = rb ^ (rb >> 16);
+                put(dst[i0] + idx, cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)));
+                if constexpr (i1 < LT::Q)
+                    put(dst[i1] + idx, cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)));
+            });
+            return;
+        }
+    }
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        st_dev<float>(dst[i] + idx, d[i].lo());
+        st_dev<float>(dst[i] + idx + 1, d[i].hi());
+    });
+}
+
+// Two x-adjacent nodes idx, idx + 1 of a fast row (idx at an odd x) in packed
+// FP32 pairs.  A population with c_x != 0 streams in from x - c_x, an even
+// element offset for both nodes together: one 32-bit (16-bit storage) or
+// 64-bit (FP32) load; the c_x = 0 populations take two scalar loads.  The
+// arithmetic is the scalar node's, lane by lane.
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
+    const Geom &g = a.g;
+    F2 d[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        const S *p = a.src[i] + idx;
+        if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
+        else d[i] = ld_pair<S>(p);
+    });
+    const F2 Fx(a.F[0]), Fy(a.F[1]), Fz(a.F[2]);
+    Mom<F2> m = moments<LT>(d);
+    F2 ux, uy, uz;
+    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    if (!(m.drho.lo() > -0.9f && m.drho.lo() < 9.0f && m.drho.hi() > -0.9f && m.drho.hi() < 9.0f))
+        atomicOr(a.status, 1);
+    collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, F2(a.om1), Fx, Fy, Fz);
+    store_pair<LT, S>(a.dst, idx, d, g.sround != 0, sr_seed(idx, m.drho.lo(), ux.lo()),
+                      sr_seed(idx + 1u, m.drho.hi(), ux.hi()));
+}
+
+// one work item (one warp) of the tile step; A is TileArgs wherever it lives
+// (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
+// DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
+// applies the walls and writes the velocity field; MODE 2 streams again,
+// takes tau_t from the 7-point stencil of that field and collides.
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
+__device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
+    // the packed-pair form: 16- and 32-bit storage, the DNS step with a
+    // uniform force and the RR collision (the host sets a.pairs only then,
+    // and only for an even nx)
+    constexpr bool PAIRABLE = sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
+    if (item >= a.nitems) return;
+    bool pair = false;
+    const Geom &g = a.g;
+    uint32_t row;
+    int x, y, z;
+    bool fast;
+    // the slow items go first so that they overlap the bulk instead of
+    // forming a tail: the edge items, then the rows of the last z plane (the
+    // row order is rotated by one plane)
+    const uint32_t nedge_items = a.nitems - a.nmain;
+    if (item >= nedge_items) {
+        const uint32_t mitem = item - nedge_items;
+        const uint32_t grp = fdiv(mitem, a.div_group);
+        const uint32_t sub = mitem - grp * a.group_items;
+        bool xface = false;
+        if (sub < a.rows_group * a.segs) {
+            const uint32_t rl = fdiv(sub, a.div_segs);
+            row = grp * a.rows_group + rl;
+            const uint32_t col = (sub - rl * a.segs) * 32u + lane;
+            if constexpr (PAIRABLE) pair = a.pairs != 0;
+            // pairs (1 + 2 col, 2 + 2 col): an even nx has an even number of
+            // interior nodes, so the pairs cover x in [1, nx-2] exactly
+            x = 1 + (int)(pair ? 2u * col : col);
+            fast = true;
+            if (x > g.nx - 2) return;
+        } else {
+            // the x = 0 nodes of the group's rows, 32 per item, then the
+            // x = nx-1 nodes: whole CTAs of these slower items
+            const uint32_t xi = sub - a.rows_group * a.segs;
+            const bool lo = xi < a.xf_half;
+            row = grp * a.rows_group + (lo ? xi : xi - a.xf_half) * 32u + lane;
+            x = lo ? 0 : g.nx - 1;
+            fast = false;
+            xface = true;
+        }
+        if (row >= a.nrows) return;
+        row += a.rot;
+        if (row >= a.nrows) row -= a.nrows;
+        z = (int)fdiv(row, a.div_ny);
+        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+        const bool yzw = ((a.yzwall & 1u) && y == 0) || ((a.yzwall & 2u) && y == g.ny - 1) ||
+                         ((a.yzwall & 4u) && z == 0) || ((a.yzwall & 8u) && z == g.nz - 1);
+        if (xface && yzw) return; // an edge node: handled by the edge items
+        fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
+    } else {
+        const uint32_t e = item * 32u + lane;
+        if (e >= a.nedges) return;
+        const uint32_t nidx = a.edges[e];
+        row = fdiv(nidx, a.div_nx);
+        x = (int)(nidx - row * (uint32_t)g.nx);
+        z = (int)fdiv(row, a.div_ny);
+        y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+        fast = false;
+    }
+    if constexpr (PAIRABLE) {
+        if (pair && fast) {
+            pair_node<LT, S, FORCE>(a, row * (uint32_t)g.nx + (uint32_t)x);
+            return;
+        }
+    }
+    // a row on a y/z face or a periodic edge row in the pair layout: its two
+    // nodes one after the other through the general node path
+    const int nn = pair ? 2 : 1;
+#pragma unroll 1
+    for (int k = 0; k < nn; k++) tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x + k, y, z, fast);
+}
+
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
-__global__ void __launch_bounds__(256, tile_min_blocks<S, FORCE, MODE>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(256, tile_min_blocks<S, MODE, FIELD, BGK>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
     tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
 

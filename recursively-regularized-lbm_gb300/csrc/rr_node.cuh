@@ -19,9 +19,19 @@
 // Hermite coefficients are merged before the per-pair evaluation.
 #pragma once
 
+#include <cmath>
+
 #include "rr_lattice.cuh"
 
 namespace rr {
+
+// a * b + c with one rounding, for every compute type of the node arithmetic
+// (the packed FP32 pair of rr_pair.cuh has its own overload).  The FP32
+// kernels are compiled without automatic multiply-add contraction, so that a
+// node computed alone and a node computed in a packed pair go through the
+// same roundings; the products that should fuse say so here.
+__host__ __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+__host__ __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
 
 template <typename T>
 struct Mom {
@@ -82,7 +92,7 @@ __host__ __device__ __forceinline__ T even_poly(const T (&A)[6]) {
             } else if constexpr (h == -1.0) {
                 s = first ? -A[k] : s - A[k];
             } else {
-                s = first ? T(h) * A[k] : s + T(h) * A[k];
+                s = first ? T(h) * A[k] : fma_(T(h), A[k], s);
             }
             first = false;
         }
@@ -100,7 +110,7 @@ __host__ __device__ __forceinline__ T odd_poly(const T (&B)[10]) {
         if (h == 0.0) return;
         if (h == 1.0) s = first ? v : s + v;
         else if (h == -1.0) s = first ? -v : s - v;
-        else s = first ? T(h) * v : s + T(h) * v;
+        else s = first ? T(h) * v : fma_(T(h), v, s);
         first = false;
     };
     if constexpr (LINEAR) {
@@ -122,12 +132,13 @@ __host__ __device__ __forceinline__ T odd_poly(const T (&B)[10]) {
 template <typename T>
 __host__ __device__ __forceinline__ void aneq_base(const Mom<T> &m, T rho, T ux, T uy, T uz, T (&n)[6]) {
     const T r3 = T(3) * rho;
-    n[0] = T(3) * m.pxy - r3 * ux * uy;
-    n[1] = T(3) * m.pxz - r3 * ux * uz;
-    n[2] = T(3) * m.pyz - r3 * uy * uz;
-    n[3] = T(3) * m.pxx - m.drho - r3 * ux * ux;
-    n[4] = T(3) * m.pyy - m.drho - r3 * uy * uy;
-    n[5] = T(3) * m.pzz - m.drho - r3 * uz * uz;
+    const T rx = -(r3 * ux), ry = -(r3 * uy), rz = -(r3 * uz);
+    n[0] = fma_(rx, uy, T(3) * m.pxy);
+    n[1] = fma_(rx, uz, T(3) * m.pxz);
+    n[2] = fma_(ry, uz, T(3) * m.pyz);
+    n[3] = fma_(rx, ux, fma_(T(3), m.pxx, -m.drho));
+    n[4] = fma_(ry, uy, fma_(T(3), m.pyy, -m.drho));
+    n[5] = fma_(rz, uz, fma_(T(3), m.pzz, -m.drho));
 }
 
 // third-order coefficients (recursive a3neq, collision.cu:88-94) scaled for
@@ -136,13 +147,14 @@ template <typename T>
 __host__ __device__ __forceinline__ void third_from_second(const T (&n)[6], T ux, T uy, T uz, T scale,
                                                   T (&B)[10]) {
     const T s15 = T(1.5) * scale;
-    B[0] = s15 * (n[3] * uy + T(2) * ux * n[0]); // 210
-    B[1] = s15 * (n[3] * uz + T(2) * ux * n[1]); // 201
-    B[2] = s15 * (n[4] * uz + T(2) * uy * n[2]); // 021
-    B[3] = s15 * (n[4] * ux + T(2) * uy * n[0]); // 120
-    B[4] = s15 * (n[5] * uy + T(2) * uz * n[2]); // 012
-    B[5] = s15 * (n[5] * ux + T(2) * uz * n[1]); // 102
-    B[6] = T(9) * scale * (n[0] * uz + n[1] * uy + n[2] * ux);
+    const T x2 = T(2) * ux, y2 = T(2) * uy, z2 = T(2) * uz;
+    B[0] = s15 * fma_(n[3], uy, x2 * n[0]); // 210
+    B[1] = s15 * fma_(n[3], uz, x2 * n[1]); // 201
+    B[2] = s15 * fma_(n[4], uz, y2 * n[2]); // 021
+    B[3] = s15 * fma_(n[4], ux, y2 * n[0]); // 120
+    B[4] = s15 * fma_(n[5], uy, z2 * n[2]); // 012
+    B[5] = s15 * fma_(n[5], ux, z2 * n[1]); // 102
+    B[6] = (T(9) * scale) * fma_(n[0], uz, fma_(n[1], uy, n[2] * ux));
 }
 
 // equilibrium Hermite coefficients: A = rho u^ u^ (3 rho u_a u_b), b = (sqrt3/2)
@@ -150,22 +162,24 @@ __host__ __device__ __forceinline__ void third_from_second(const T (&n)[6], T ux
 template <typename T>
 __host__ __device__ __forceinline__ void eq_coeffs(T rho, T ux, T uy, T uz, T (&A)[6], T (&B)[10]) {
     const T r3 = T(3) * rho, r45 = T(4.5) * rho;
-    A[0] = r3 * ux * uy;
-    A[1] = r3 * ux * uz;
-    A[2] = r3 * uy * uz;
-    A[3] = r3 * ux * ux;
-    A[4] = r3 * uy * uy;
-    A[5] = r3 * uz * uz;
-    B[0] = r45 * ux * ux * uy;
-    B[1] = r45 * ux * ux * uz;
-    B[2] = r45 * uy * uy * uz;
-    B[3] = r45 * uy * uy * ux;
-    B[4] = r45 * uz * uz * uy;
-    B[5] = r45 * uz * uz * ux;
-    B[6] = T(27) * rho * ux * uy * uz;
-    B[7] = r3 * ux;
-    B[8] = r3 * uy;
-    B[9] = r3 * uz;
+    const T rx = r3 * ux, ry = r3 * uy, rz = r3 * uz;
+    const T qx = r45 * ux * ux, qy = r45 * uy * uy, qz = r45 * uz * uz;
+    A[0] = rx * uy;
+    A[1] = rx * uz;
+    A[2] = ry * uz;
+    A[3] = rx * ux;
+    A[4] = ry * uy;
+    A[5] = rz * uz;
+    B[0] = qx * uy;
+    B[1] = qx * uz;
+    B[2] = qy * uz;
+    B[3] = qy * ux;
+    B[4] = qz * uy;
+    B[5] = qz * ux;
+    B[6] = T(9) * A[0] * uz;
+    B[7] = rx;
+    B[8] = ry;
+    B[9] = rz;
 }
 
 // Force correction sum_i H2_ab,i Fbar_i feq_i (the f + Fbar feq term of
@@ -225,7 +239,7 @@ __host__ __device__ __forceinline__ void collide_generic(T (&d)[LT::Q], const Mo
         // merged coefficients: rho a2 + (1 - 1/tau) a2neq, same for third order
         T A[6], B[10];
 #pragma unroll
-        for (int k = 0; k < 6; k++) A[k] = Aq[k] + om1 * n[k];
+        for (int k = 0; k < 6; k++) A[k] = fma_(om1, n[k], Aq[k]);
         T Bn[10];
         third_from_second(n, ux, uy, uz, om1, Bn);
 #pragma unroll
@@ -299,9 +313,9 @@ __host__ __device__ __forceinline__ void collide(T (&d)[LT::Q], const Mom<T> &m,
 template <typename T>
 __host__ __device__ __forceinline__ void velocity(const Mom<T> &m, T Fx, T Fy, T Fz, T &ux, T &uy, T &uz) {
     const T inv = T(1) / (T(1) + m.drho);
-    ux = (m.jx + T(0.5) * Fx) * inv;
-    uy = (m.jy + T(0.5) * Fy) * inv;
-    uz = (m.jz + T(0.5) * Fz) * inv;
+    ux = fma_(T(0.5), Fx, m.jx) * inv;
+    uy = fma_(T(0.5), Fy, m.jy) * inv;
+    uz = fma_(T(0.5), Fz, m.jz) * inv;
 }
 
 // Regularized wall closure of one node (RRBC, BC.cu:4-126; Cavity

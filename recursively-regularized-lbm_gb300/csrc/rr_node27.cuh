@@ -43,17 +43,17 @@ __host__ __device__ __forceinline__ Mom<T> moments27(const T (&d)[27]) {
     const T Jx_c = ga + gb, Jy_c = ga - gb, Jz_c = gc + ge;
     Mom<T> m;
     const T Se = Sxy + Sxz + Syz;
-    m.drho = w0 * d[0] + w1 * (sx + sy + sz) + w2 * Se + w3 * Sc;
-    m.jx = w1 * gx + w2 * (Jx_xy + Jx_xz) + w3 * Jx_c;
-    m.jy = w1 * gy + w2 * (Jy_xy + Jy_yz) + w3 * Jy_c;
-    m.jz = w1 * gz + w2 * (Jz_xz + Jz_yz) + w3 * Jz_c;
     const T c3 = w3 * Sc;
-    m.pxx = w1 * sx + w2 * (Sxy + Sxz) + c3;
-    m.pyy = w1 * sy + w2 * (Sxy + Syz) + c3;
-    m.pzz = w1 * sz + w2 * (Sxz + Syz) + c3;
-    m.pxy = w2 * Dxy + w3 * Pxy_c;
-    m.pxz = w2 * Dxz + w3 * Pxz_c;
-    m.pyz = w2 * Dyz + w3 * Pyz_c;
+    m.drho = fma_(w0, d[0], fma_(w1, sx + sy + sz, fma_(w2, Se, c3)));
+    m.jx = fma_(w1, gx, fma_(w2, Jx_xy + Jx_xz, w3 * Jx_c));
+    m.jy = fma_(w1, gy, fma_(w2, Jy_xy + Jy_yz, w3 * Jy_c));
+    m.jz = fma_(w1, gz, fma_(w2, Jz_xz + Jz_yz, w3 * Jz_c));
+    m.pxx = fma_(w1, sx, fma_(w2, Sxy + Sxz, c3));
+    m.pyy = fma_(w1, sy, fma_(w2, Sxy + Syz, c3));
+    m.pzz = fma_(w1, sz, fma_(w2, Sxz + Syz, c3));
+    m.pxy = fma_(w2, Dxy, w3 * Pxy_c);
+    m.pxz = fma_(w2, Dxz, w3 * Pxz_c);
+    m.pyz = fma_(w2, Dyz, w3 * Pyz_c);
     return m;
 }
 
@@ -74,23 +74,23 @@ __host__ __device__ __forceinline__ void collide27(T (&d)[27], const Mom<T> &m, 
     T Aq[6], Bq[10], Bn[10];
     eq_coeffs(rho, ux, uy, uz, Aq, Bq);
     third_from_second(n, ux, uy, uz, om1, Bn);
-    const T A0 = Aq[0] + om1 * n[0], A1 = Aq[1] + om1 * n[1], A2 = Aq[2] + om1 * n[2];
-    const T A3 = Aq[3] + om1 * n[3], A4 = Aq[4] + om1 * n[4], A5 = Aq[5] + om1 * n[5];
+    const T A0 = fma_(om1, n[0], Aq[0]), A1 = fma_(om1, n[1], Aq[1]), A2 = fma_(om1, n[2], Aq[2]);
+    const T A3 = fma_(om1, n[3], Aq[3]), A4 = fma_(om1, n[4], Aq[4]), A5 = fma_(om1, n[5], Aq[5]);
     const T b210 = Bq[0] + Bn[0], b201 = Bq[1] + Bn[1], b021 = Bq[2] + Bn[2];
     const T b120 = Bq[3] + Bn[3], b012 = Bq[4] + Bn[4], b102 = Bq[5] + Bn[5];
     const T t111 = Bq[6] + Bn[6];
     // even parts
     const T hx = T(1.5) * A3, hy = T(1.5) * A4, hz = T(1.5) * A5;
     const T txy = T(3) * A0, txz = T(3) * A1, tyz = T(3) * A2;
-    const T K0 = K - T(0.5) * (A3 + A4 + A5);
+    const T K0 = fma_(T(-0.5), A3 + A4 + A5, K);
     const T Kx = K0 + hx, Ky = K0 + hy, Kz = K0 + hz;
     const T Exy = Kx + hy, Exz = Kx + hz, Eyz = Ky + hz;
     const T Ec = Exy + hz;
     // odd parts
     const T X00 = Bq[7] - b120 - b102, Y00 = Bq[8] - b210 - b012, Z00 = Bq[9] - b201 - b021;
-    const T X10 = X00 + T(3) * b120, X01 = X00 + T(3) * b102, X11 = X10 + T(3) * b102;
-    const T Y10 = Y00 + T(3) * b210, Y01 = Y00 + T(3) * b012, Y11 = Y10 + T(3) * b012;
-    const T Z10 = Z00 + T(3) * b201, Z01 = Z00 + T(3) * b021, Z11 = Z10 + T(3) * b021;
+    const T X10 = fma_(T(3), b120, X00), X01 = fma_(T(3), b102, X00), X11 = fma_(T(3), b102, X10);
+    const T Y10 = fma_(T(3), b210, Y00), Y01 = fma_(T(3), b012, Y00), Y11 = fma_(T(3), b012, Y10);
+    const T Z10 = fma_(T(3), b201, Z00), Z01 = fma_(T(3), b021, Z00), Z11 = fma_(T(3), b021, Z10);
     T e, o;
     d[0] = K0;
     d[1] = Kx + X00;

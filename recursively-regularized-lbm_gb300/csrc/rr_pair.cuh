@@ -1,0 +1,66 @@
+// rr_pair.cuh -- two lattice nodes per thread in packed FP32 pairs.
+//
+// The node arithmetic of rr_node.cuh is written once over its compute type
+// T.  F2 is a pair of FP32 values (two x-adjacent nodes) whose operations map
+// to the packed FP32x2 instructions of sm_100-family GPUs (add/sub/mul/fma
+// .rn.f32x2): one instruction does the work of two scalar FP32 instructions,
+// which halves the issue slots the collision takes.  Each lane of an F2
+// operation rounds exactly as the scalar FP32 operation does, and the FP32
+// kernels are compiled without automatic multiply-add contraction, so a node
+// computed in a pair gets the same bits as the same node computed alone.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace rr {
+
+struct F2 {
+    float2 v;
+    F2() = default;
+    __device__ __forceinline__ explicit F2(float2 a) : v(a) {}
+    __device__ __forceinline__ F2(float a, float b) : v(make_float2(a, b)) {}
+    // a constant in both lanes
+    __device__ __forceinline__ explicit F2(double c) : v(make_float2((float)c, (float)c)) {}
+    __device__ __forceinline__ explicit F2(float c) : v(make_float2(c, c)) {}
+    __device__ __forceinline__ explicit F2(int c) : v(make_float2((float)c, (float)c)) {}
+    __device__ __forceinline__ float lo() const { return v.x; }
+    __device__ __forceinline__ float hi() const { return v.y; }
+};
+
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+    unsigned long long r;
+    const unsigned long long x = *reinterpret_cast<const unsigned long long *>(&a.v);
+    const unsigned long long y = *reinterpret_cast<const unsigned long long *>(&b.v);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+    return F2(*reinterpret_cast<const float2 *>(&r));
+}
+__device__ __forceinline__ F2 operator-(F2 a) { return F2(make_float2(-a.v.x, -a.v.y)); }
+// IEEE division lane by lane (as the scalar FP32 division)
+__device__ __forceinline__ F2 operator/(F2 a, F2 b) {
+    return F2(make_float2(__fdiv_rn(a.v.x, b.v.x), __fdiv_rn(a.v.y, b.v.y)));
+}
+__device__ __forceinline__ F2 &operator+=(F2 &a, F2 b) { return a = a + b; }
+__device__ __forceinline__ F2 &operator-=(F2 &a, F2 b) { return a = a - b; }
+__device__ __forceinline__ F2 &operator*=(F2 &a, F2 b) { return a = a * b; }
+__device__ __forceinline__ F2 fma_(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+
+// two consecutive stored populations (the first at an even element offset)
+// as an FP32 pair
+template <typename S> __device__ __forceinline__ F2 ld_pair(const S *p);
+template <> __device__ __forceinline__ F2 ld_pair(const float *p) {
+    return F2(*reinterpret_cast<const float2 *>(p));
+}
+template <> __device__ __forceinline__ F2 ld_pair(const __half *p) {
+    return F2(__half22float2(*reinterpret_cast<const __half2 *>(p)));
+}
+template <> __device__ __forceinline__ F2 ld_pair(const __nv_bfloat16 *p) {
+    return F2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(p)));
+}
+
+} // namespace rr

