@@ -91,6 +91,12 @@ def lib():
         L.orc_trip_force.argtypes = [ctypes.POINTER(Params), ctypes.c_longlong, ctypes.c_double, dp, dp, dp]
         L.orc_run_trip.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_State), ctypes.POINTER(Trip),
                                    ctypes.c_int]
+        cp, li = ctypes.c_char_p, ctypes.c_long
+        L.orc_out_diag.argtypes = [cp, ctypes.c_int, li, dp, dp, dp, dp, ctypes.c_double]
+        L.orc_out_flow.argtypes = [cp, ctypes.c_int, li, dp, dp, dp, dp]
+        L.orc_out_profile.argtypes = [cp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp,
+                                      ctypes.c_double]
+        L.orc_out_f.argtypes = [cp, ctypes.c_int, ctypes.c_int, li, dp]
         _LIB = L
     return _LIB
 
@@ -218,3 +224,22 @@ def tg_reference_params(L=100, q=27):
     visc = U0 * L / Re0
     tau = visc / (1.0 / 3.0) + 0.5
     return U0, visc, tau
+
+
+def write_outputs(directory, istep, rho, ux, uy, uz, taut, f, ustar, ystar):
+    """The reference's four writers (output.cu, restated in the oracle) on
+    FP64 fields of shape (nz, ny, nx) and f of shape (q, nz, ny, nx), into
+    directory; the console line of diag_flow goes to stdout."""
+    L = lib()
+    d = str(directory).encode()
+    nz, ny, nx = rho.shape
+    n = rho.size
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (rho, ux, uy, uz, taut)]
+    fa = np.ascontiguousarray(f, dtype=np.float64)
+    ok = (L.orc_out_diag(d, int(istep), n, _p(a[0]), _p(a[1]), _p(a[2]), _p(a[3]), float(ustar)) == 0
+          and L.orc_out_flow(d, int(istep), n, _p(a[0]), _p(a[1]), _p(a[2]), _p(a[3])) == 0
+          and L.orc_out_profile(d, int(istep), nx, ny, nz, _p(a[1]), _p(a[2]), _p(a[3]), _p(a[4]),
+                                float(ystar)) == 0
+          and L.orc_out_f(d, int(istep), fa.shape[0], n, _p(fa)) == 0)
+    if not ok:
+        raise OSError(f"cannot write the outputs into {directory}")

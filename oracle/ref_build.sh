@@ -1,6 +1,7 @@
 #!/bin/sh
-# Compiles the reference channel kernels for the host, from their own sources
-# where they lie, into oracle/_ref/ (TEST INFRASTRUCTURE ONLY).
+# Compiles the reference channel kernels and output routines for the host,
+# from their own sources where they lie, into oracle/_ref/ (TEST
+# INFRASTRUCTURE ONLY).
 #   ref_build.sh [REFDIR] [LX LY LZ USE_LES] ...
 # The grid and the DNS/LES switch are compile-time macros of the reference
 # (parameters.h); a pre-included header with the same include guard sets them.
@@ -77,6 +78,17 @@ EOP
         "$HERE/ref_driver_bgk.cpp" -o "$OUT/$NAME"
     echo "built $OUT/$NAME"
 }
+# the output routines (output.cu) with their globals, one grid
+build_out() {
+    LX=$1; LY=$2; LZ=$3; LES=$4
+    NAME="libref_out_${LX}x${LY}x${LZ}_les${LES}.so"
+    P="$OUT/params_${LX}x${LY}x${LZ}_les${LES}.h"
+    [ -f "$P" ] || { echo "build_one $LX $LY $LZ $LES first" >&2; exit 1; }
+    $CXX -O2 -fPIC -std=c++14 -w -shared \
+        -I "$HERE/ref_shim" -I "$REF" -include "$P" -x c++ \
+        "$REF/globals.cu" "$REF/output.cu" "$HERE/ref_output_driver.cpp" -o "$OUT/$NAME"
+    echo "built $OUT/$NAME"
+}
 if [ $# -ge 4 ]; then
     while [ $# -ge 4 ]; do build_one "$1" "$2" "$3" "$4"; shift 4; done
 else
@@ -84,4 +96,5 @@ else
     build_one 16 12 8 0
     build_one 16 12 8 1
     build_bgk 16 12 8
+    build_out 16 12 8 1
 fi

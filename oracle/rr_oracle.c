@@ -9,6 +9,7 @@
 #include "rr_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -1022,4 +1023,106 @@ void orc_init_channel_config(const orc_params *P, double uc, double amp, uint64_
             }
     (void)N;
     orc_init_equilibrium2(P, f, rho, ux, uy, uz);
+}
+
+
+/* ---- the reference's file writers (output.cu) -------------------------- */
+
+static FILE *orc_open(const char *dir, const char *name, const char *mode) {
+    char path[1024];
+    snprintf(path, sizeof path, "%s/%s", dir, name);
+    return fopen(path, mode);
+}
+
+/* output.cu:24-56: sums in index order, then the console line and the
+ * statistics.dat line */
+int orc_out_diag(const char *dir, int istep, long n, const double *rho, const double *ux, const double *uy,
+                 const double *uz, double u0) {
+    double umean = 0.0, vmean = 0.0, wmean = 0.0, rhomean = 0.0;
+    for (long i = 0; i < n; i++) {
+        umean += ux[i];
+        vmean += uy[i];
+        wmean += uz[i];
+        rhomean += rho[i];
+    }
+    umean /= n;
+    vmean /= n;
+    wmean /= n;
+    rhomean /= n;
+    printf("Step %-7d umean = %.17e, vmean = %.17e, wmean = %.17e, rhomean = %14.6e\n", istep, umean / u0, vmean,
+           wmean, rhomean);
+    fflush(stdout);
+    FILE *fp = orc_open(dir, "statistics.dat", "a");
+    if (!fp) return -1;
+    const int w = fprintf(fp, "%-7d %14.6e %14.6e %14.6e %14.6e\n", istep, umean, vmean, wmean, rhomean);
+    fclose(fp);
+    return w < 0 ? -1 : 0;
+}
+
+/* output.cu:89-131: rho, ux, uy, uz back to back */
+int orc_out_flow(const char *dir, int istep, long n, const double *rho, const double *ux, const double *uy,
+                 const double *uz) {
+    char name[64];
+    snprintf(name, sizeof name, "%09d.dat", istep);
+    FILE *fp = orc_open(dir, name, "wb");
+    if (!fp) return -1;
+    const double *a[4] = {rho, ux, uy, uz};
+    int ok = 1;
+    for (int k = 0; k < 4; k++) ok = ok && fwrite(a[k], sizeof(double), (size_t)n, fp) == (size_t)n;
+    fclose(fp);
+    return ok ? 0 : -1;
+}
+
+/* output.cu:158-214: per y plane, the means over x (outer) and z (inner),
+ * then the second moments of the fluctuations in the same order */
+int orc_out_profile(const char *dir, int istep, int nx, int ny, int nz, const double *ux, const double *uy,
+                    const double *uz, const double *taut, double ystar) {
+    FILE *fp = orc_open(dir, "Profiles.txt", "a");
+    if (!fp) return -1;
+    fprintf(fp, "%d\n", istep);
+    for (int iy = 0; iy < ny; iy++) {
+        double su = 0.0, sv = 0.0, sw = 0.0, st = 0.0;
+        double s_uu = 0, s_vv = 0, s_ww = 0, s_uv = 0, s_uw = 0, s_vw = 0;
+        int count = 0;
+        for (int ix = 0; ix < nx; ix++)
+            for (int iz = 0; iz < nz; iz++) {
+                const long idx = ((long)iz * ny + iy) * nx + ix;
+                su += ux[idx];
+                sv += uy[idx];
+                sw += uz[idx];
+                st += taut[idx];
+                count++;
+            }
+        const double au = su / count, av = sv / count, aw = sw / count;
+        (void)st;
+        for (int ix = 0; ix < nx; ix++)
+            for (int iz = 0; iz < nz; iz++) {
+                const long idx = ((long)iz * ny + iy) * nx + ix;
+                const double ur = ux[idx] - au, vr = uy[idx] - av, wr = uz[idx] - aw;
+                s_uu += ur * ur;
+                s_vv += vr * vr;
+                s_ww += wr * wr;
+                s_uv += ur * vr;
+                s_uw += ur * wr;
+                s_vw += vr * wr;
+            }
+        fprintf(fp, "%d, %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e %14.6e\n", iy,
+                iy + 0.5, (iy + 0.5) / ystar, au, av, aw, s_uu / count, s_vv / count, s_ww / count, s_uv / count,
+                s_uw / count, s_vw / count);
+    }
+    const int e = fflush(fp);
+    fclose(fp);
+    return e == 0 ? 0 : -1;
+}
+
+/* output.cu:227-258: all populations, reference layout */
+int orc_out_f(const char *dir, int istep, int q, long n, const double *f) {
+    char name[64];
+    snprintf(name, sizeof name, "f%09d.dat", istep);
+    FILE *fp = orc_open(dir, name, "wb");
+    if (!fp) return -1;
+    const size_t cnt = (size_t)q * (size_t)n;
+    const int ok = fwrite(f, sizeof(double), cnt, fp) == cnt;
+    fclose(fp);
+    return ok ? 0 : -1;
 }

@@ -178,6 +178,28 @@ void orc_init_channel_config(const orc_params *P, double uc, double amp, uint64_
 
 void orc_set_threads(int n);
 
+/* The reference's file writers (RR27V33_code_DNS_LES/output.cu) restated,
+ * writing into directory dir (the reference writes into ./data): fields of
+ * n = nx ny nz nodes in the reference layout, f of q n values.  Return 0, or
+ * -1 if a file cannot be written.
+ *   orc_out_diag     diag_flow (output.cu:3-66): the console line on stdout
+ *                    and a line appended to statistics.dat; u0 = the friction
+ *                    velocity the console divides umean by
+ *   orc_out_flow     output_flow (output.cu:68-140): %09d.dat, rho ux uy uz
+ *   orc_out_profile  output_profile (output.cu:142-225): Profiles.txt; the
+ *                    reference hands iy + 0.5 to a %d conversion, so its
+ *                    first column is whatever integer the variadic call
+ *                    leaves there and the eleven %e columns print the first
+ *                    eleven doubles; here the first column is iy
+ *   orc_out_f        output_f (output.cu:227-258): f%09d.dat */
+int orc_out_diag(const char *dir, int istep, long n, const double *rho, const double *ux, const double *uy,
+                 const double *uz, double u0);
+int orc_out_flow(const char *dir, int istep, long n, const double *rho, const double *ux, const double *uy,
+                 const double *uz);
+int orc_out_profile(const char *dir, int istep, int nx, int ny, int nz, const double *ux, const double *uy,
+                    const double *uz, const double *taut, double ystar);
+int orc_out_f(const char *dir, int istep, int q, long n, const double *f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -306,6 +306,7 @@ template <class LT, typename T, bool FORCE>
 __host__ __device__ __forceinline__ void collide(T (&d)[LT::Q], const Mom<T> &m, T drho_eq, T ux, T uy,
                                                  T uz, T om1, T Fx, T Fy, T Fz) {
     if constexpr (LT::Q == 27 && !FORCE) collide27(d, m, drho_eq, ux, uy, uz, om1);
+    else if constexpr (LT::Q == 27) collide27_forced(d, m, drho_eq, ux, uy, uz, om1, Fx, Fy, Fz);
     else collide_generic<LT, T, FORCE>(d, m, drho_eq, ux, uy, uz, om1, Fx, Fy, Fz);
 }
 

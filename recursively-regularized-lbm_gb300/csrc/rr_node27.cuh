@@ -57,37 +57,28 @@ __host__ __device__ __forceinline__ Mom<T> moments27(const T (&d)[27]) {
     return m;
 }
 
-// Force-free RR collision (collision.cu:41-119 with F = 0).  With A = rho a2 +
-// (1 - 1/tau) a2neq and b, t111 the merged third-order coefficients, the new
-// deviation of population i is  even_i + odd_i  with
-//   even_i = drho + 1/2 sec_i(A)
+// Every population of a D3Q27 node from Hermite coefficients: with K the
+// density deviation, A (110, 101, 011, 200, 020, 002) the second-order and
+// b (210, 201, 021, 120, 012, 102), t111 the third-order coefficients and L
+// = 3 rho u the linear ones, population i is  even_i + odd_i  with
+//   even_i = K + 1/2 sec_i(A)
 //          = K0 + 1.5 sum_{a: c_a != 0} A_aa + 3 sum_{a<b} c_a c_b A_ab
-//   odd_i  = 3 rho c.u + 1/2 thir_i(B)
+//   odd_i  = c.L + 1/2 thir_i(B)
 //          = c_x X + c_y Y + c_z Z + c_x c_y c_z t111,
-//   X = 3 rho u_x + (3 c_y^2 - 1) b120 + (3 c_z^2 - 1) b102   (Y, Z likewise).
+//   X = L_x + (3 c_y^2 - 1) b120 + (3 c_z^2 - 1) b102   (Y, Z likewise).
 template <typename T>
-__host__ __device__ __forceinline__ void collide27(T (&d)[27], const Mom<T> &m, T K, T ux, T uy, T uz,
-                                                   T om1) {
-    const T rho = T(1) + K;
-    T n[6];
-    aneq_base(m, rho, ux, uy, uz, n);
-    T Aq[6], Bq[10], Bn[10];
-    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
-    third_from_second(n, ux, uy, uz, om1, Bn);
-    const T A0 = fma_(om1, n[0], Aq[0]), A1 = fma_(om1, n[1], Aq[1]), A2 = fma_(om1, n[2], Aq[2]);
-    const T A3 = fma_(om1, n[3], Aq[3]), A4 = fma_(om1, n[4], Aq[4]), A5 = fma_(om1, n[5], Aq[5]);
-    const T b210 = Bq[0] + Bn[0], b201 = Bq[1] + Bn[1], b021 = Bq[2] + Bn[2];
-    const T b120 = Bq[3] + Bn[3], b012 = Bq[4] + Bn[4], b102 = Bq[5] + Bn[5];
-    const T t111 = Bq[6] + Bn[6];
+__host__ __device__ __forceinline__ void eval27(T (&d)[27], T K, const T (&A)[6], const T (&b)[6], T t111, T Lx,
+                                                T Ly, T Lz) {
+    const T b210 = b[0], b201 = b[1], b021 = b[2], b120 = b[3], b012 = b[4], b102 = b[5];
     // even parts
-    const T hx = T(1.5) * A3, hy = T(1.5) * A4, hz = T(1.5) * A5;
-    const T txy = T(3) * A0, txz = T(3) * A1, tyz = T(3) * A2;
-    const T K0 = fma_(T(-0.5), A3 + A4 + A5, K);
+    const T hx = T(1.5) * A[3], hy = T(1.5) * A[4], hz = T(1.5) * A[5];
+    const T txy = T(3) * A[0], txz = T(3) * A[1], tyz = T(3) * A[2];
+    const T K0 = fma_(T(-0.5), A[3] + A[4] + A[5], K);
     const T Kx = K0 + hx, Ky = K0 + hy, Kz = K0 + hz;
     const T Exy = Kx + hy, Exz = Kx + hz, Eyz = Ky + hz;
     const T Ec = Exy + hz;
     // odd parts
-    const T X00 = Bq[7] - b120 - b102, Y00 = Bq[8] - b210 - b012, Z00 = Bq[9] - b201 - b021;
+    const T X00 = Lx - b120 - b102, Y00 = Ly - b210 - b012, Z00 = Lz - b201 - b021;
     const T X10 = fma_(T(3), b120, X00), X01 = fma_(T(3), b102, X00), X11 = fma_(T(3), b102, X10);
     const T Y10 = fma_(T(3), b210, Y00), Y01 = fma_(T(3), b012, Y00), Y11 = fma_(T(3), b012, Y10);
     const T Z10 = fma_(T(3), b201, Z00), Z01 = fma_(T(3), b021, Z00), Z11 = fma_(T(3), b021, Z10);
@@ -111,6 +102,88 @@ __host__ __device__ __forceinline__ void collide27(T (&d)[27], const Mom<T> &m, 
     e = Em + dd; o = P - Qp; d[23] = e + o; d[21] = e - o;
     e = Em - dd; o = M + R; d[22] = e + o; d[24] = e - o;
     e = Ep - s; o = M - R; d[26] = e + o; d[20] = e - o;
+}
+
+// Force-free RR collision (collision.cu:41-119 with F = 0): the populations
+// of A = rho a2 + (1 - 1/tau) a2neq and the merged third-order coefficients.
+template <typename T>
+__host__ __device__ __forceinline__ void collide27(T (&d)[27], const Mom<T> &m, T K, T ux, T uy, T uz,
+                                                   T om1) {
+    const T rho = T(1) + K;
+    T n[6];
+    aneq_base(m, rho, ux, uy, uz, n);
+    T Aq[6], Bq[10], Bn[10];
+    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
+    third_from_second(n, ux, uy, uz, om1, Bn);
+    T A[6], b[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        A[k] = fma_(om1, n[k], Aq[k]);
+        b[k] = Bq[k] + Bn[k];
+    }
+    eval27(d, K, A, b, Bq[6] + Bn[6], Bq[7], Bq[8], Bq[9]);
+}
+
+// Forced RR collision (collision.cu:24-119): with E_i the equilibrium
+// deviation (feq_i / w_i - 1) and Fbar_i = 1/2 (c_i - u).F / cs^2, the
+// reference's
+//   a2neq = sum_i H2_i (f_i + Fbar_i feq_i) - rho u u,
+//   f*_i  = feq_i + (1 - 1/tau) fneq_i + Fbar_i feq_i
+// become, in deviations, with g_i = (1 + E_i) Fbar_i,
+//   a2neq = (the force-free a2neq) + sum_i w_i H2_i g_i,
+//   d*_i  = [K + even_i(Aq + (1 - 1/tau) a2neq) + odd_i(Bq + Bn)] + g_i,
+// the bracket being the force-free form with the corrected a2neq: two
+// evaluations of all populations (E, then the bracket) and the second
+// moments of g, instead of a pass over the pairs for the correction and
+// another for the populations.
+template <typename T>
+__host__ __device__ __forceinline__ void collide27_forced(T (&d)[27], const Mom<T> &m, T K, T ux, T uy, T uz,
+                                                          T om1, T Fx, T Fy, T Fz) {
+    const T rho = T(1) + K;
+    T n[6];
+    aneq_base(m, rho, ux, uy, uz, n);
+    T Aq[6], Bq[10];
+    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
+    const T bq[6] = {Bq[0], Bq[1], Bq[2], Bq[3], Bq[4], Bq[5]};
+    T g[27];
+    eval27(g, K, Aq, bq, Bq[6], Bq[7], Bq[8], Bq[9]); // E_i
+    // Fbar_i = Fe + 1.5 c_i.F, Fe = -1.5 u.F, by velocity class
+    const T Fe = T(-1.5) * fma_(ux, Fx, fma_(uy, Fy, uz * Fz));
+    const T fx = T(1.5) * Fx, fy = T(1.5) * Fy, fz = T(1.5) * Fz;
+    const T fxyp = fx + fy, fxym = fx - fy, fxzp = fx + fz, fxzm = fx - fz, fyzp = fy + fz, fyzm = fy - fz;
+    const T fppp = fxyp + fz, fppm = fxyp - fz, fpmp = fxym + fz, fpmm = fxym - fz;
+    T Fo[27];
+    Fo[0] = T(0);
+    Fo[1] = fx; Fo[3] = -fx; Fo[2] = fy; Fo[4] = -fy; Fo[5] = fz; Fo[6] = -fz;
+    Fo[7] = fxyp; Fo[9] = -fxyp; Fo[10] = fxym; Fo[8] = -fxym;
+    Fo[11] = fxzp; Fo[17] = -fxzp; Fo[15] = fxzm; Fo[13] = -fxzm;
+    Fo[12] = fyzp; Fo[18] = -fyzp; Fo[16] = fyzm; Fo[14] = -fyzm;
+    Fo[19] = fppp; Fo[25] = -fppp; Fo[23] = fppm; Fo[21] = -fppm;
+    Fo[22] = fpmp; Fo[24] = -fpmp; Fo[26] = fpmm; Fo[20] = -fpmm;
+#pragma unroll
+    for (int i = 0; i < 27; i++) {
+        const T Fb = i == 0 ? Fe : Fe + Fo[i];
+        g[i] = fma_(g[i], Fb, Fb); // (1 + E_i) Fbar_i
+    }
+    // sum_i w_i H2_i g_i: H2_ab = 3 c_a c_b (a != b), 3 c_a^2 - 1
+    const Mom<T> mg = moments27(g);
+    n[0] = fma_(T(3), mg.pxy, n[0]);
+    n[1] = fma_(T(3), mg.pxz, n[1]);
+    n[2] = fma_(T(3), mg.pyz, n[2]);
+    n[3] = n[3] + fma_(T(3), mg.pxx, -mg.drho);
+    n[4] = n[4] + fma_(T(3), mg.pyy, -mg.drho);
+    n[5] = n[5] + fma_(T(3), mg.pzz, -mg.drho);
+    T Bn[10];
+    third_from_second(n, ux, uy, uz, om1, Bn);
+    T A[6], b[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        A[k] = fma_(om1, n[k], Aq[k]);
+        b[k] = Bq[k] + Bn[k];
+    }
+    eval27(d, K, A, b, Bq[6] + Bn[6], Bq[7], Bq[8], Bq[9]);
+#pragma unroll
+    for (int i = 0; i < 27; i++) d[i] = d[i] + g[i];
 }
 
 } // namespace rr

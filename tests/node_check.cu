@@ -4,7 +4,8 @@
 // Built and run by tests/test_node_cpu.py; needs no GPU.
 //
 // For random post-stream states it compares, in FP64:
-//   moments27 / collide27 (factored D3Q27) with moments_generic / collide_generic
+//   moments27 / collide27 / collide27_forced (factored D3Q27) with
+//   moments_generic / collide_generic
 //   collide (D3Q27 and D3Q19, with and without body force) with orc_collide_node
 //   regularize (wall closure) with orc_regularize_node
 // and the FP32 forms with the FP64 ones.  Prints the largest differences;
@@ -74,10 +75,11 @@ static void run(const char *name, int order, double F0) {
         collide<LT, double, FORCE>(dc, m, m.drho, ux, uy, uz, 1.0 - 1.0 / tau, F[0], F[1], F[2]);
         orc_collide_node(&L, tau, F, r_o, u_o, v_o, w_o, fo);
         for (int i = 0; i < LT::Q; i++) e_col = fmax(e_col, fabs(LT::w(i) * (1.0 + dc[i]) - fo[i]));
-        if constexpr (LT::Q == 27 && !FORCE) {
+        if constexpr (LT::Q == 27) {
+            // the factored D3Q27 forms (collide27, collide27_forced) against the pair loop
             double dg[LT::Q];
             for (int i = 0; i < LT::Q; i++) dg[i] = d[i];
-            collide_generic<LT, double, false>(dg, m, m.drho, ux, uy, uz, 1.0 - 1.0 / tau, 0.0, 0.0, 0.0);
+            collide_generic<LT, double, FORCE>(dg, m, m.drho, ux, uy, uz, 1.0 - 1.0 / tau, F[0], F[1], F[2]);
             for (int i = 0; i < LT::Q; i++) e_fac = fmax(e_fac, fabs(dg[i] - dc[i]));
         }
         // FP32 path against FP64

@@ -292,3 +292,66 @@ def test_bgk_matches_reference_live():
     assert np.array_equal(s.f, f)
     for k, a in (("rho", rho), ("ux", ux), ("uy", uy), ("uz", uz)):
         assert np.array_equal(getattr(s, k), a), k
+
+
+def _out_lib():
+    path = os.path.join(ROOT, "oracle", "_ref", "libref_out_16x12x8_les1.so")
+    if not os.path.exists(path):
+        pytest.skip("reference output routines not built here (oracle/ref_build.sh needs the reference sources)")
+    R = ctypes.CDLL(path)
+    R.ref_out_ustar.restype = ctypes.c_double
+    R.ref_out_ystar.restype = ctypes.c_double
+    dp = ctypes.POINTER(ctypes.c_double)
+    R.ref_out_bind.argtypes = [dp] * 6
+    for n in ("ref_out_diag", "ref_out_flow", "ref_out_profile", "ref_out_f"):
+        getattr(R, n).argtypes = [ctypes.c_int]
+    return R
+
+
+def compare_output_dirs(a, b, istep, profile_first_column=True):
+    """the reference's four files in directories a and b: byte for byte;
+    Profiles.txt without its first column when profile_first_column is False
+    (the reference prints an unspecified integer there)"""
+    for name in ("statistics.dat", f"{istep:09d}.dat", f"f{istep:09d}.dat"):
+        with open(os.path.join(a, name), "rb") as fa, open(os.path.join(b, name), "rb") as fb:
+            assert fa.read() == fb.read(), name
+    la = open(os.path.join(a, "Profiles.txt")).read().splitlines()
+    lb = open(os.path.join(b, "Profiles.txt")).read().splitlines()
+    assert len(la) == len(lb) and la[0] == lb[0] == str(istep)
+    for x, y in zip(la[1:], lb[1:]):
+        if profile_first_column:
+            assert x == y
+        else:
+            assert x.split(",", 1)[1] == y.split(",", 1)[1]
+
+
+def test_output_writers_match_reference(tmp_path, monkeypatch, capfd):
+    """The oracle's restatement of the reference's writers against the
+    reference's output.cu compiled for the host, on the same FP64 fields of a
+    noisy 16 x 12 x 8 WALE channel after 7 steps: statistics.dat, the flow and
+    population restart files byte for byte, Profiles.txt byte for byte but
+    for its first column, and the same console line."""
+    R = _out_lib()
+    ustar, ystar = R.ref_out_ustar(), R.ref_out_ystar()
+    from helpers import load_state, oracle_for
+    from rrlbm import presets
+    p, st = presets.channel(nx=16, ny=12, nz=8, les=True, variant="config", amp=0.2)
+    assert (p.ustar, p.ystar) == (ustar, ystar)
+    o = oracle_for(p)
+    load_state(o, st)
+    o.run(7)
+    taut = o.wale()
+    fields = [np.ascontiguousarray(v) for v in (o.rho, o.ux, o.uy, o.uz, taut, o.f)]
+    a = tmp_path / "oracle"
+    a.mkdir()
+    O.write_outputs(a, 7, *fields[:5], fields[5], ustar, ystar)
+    line_a = capfd.readouterr().out
+    b = tmp_path / "ref"
+    (b / "data").mkdir(parents=True)
+    monkeypatch.chdir(b)
+    R.ref_out_bind(*[v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for v in fields])
+    for fn in (R.ref_out_diag, R.ref_out_flow, R.ref_out_profile, R.ref_out_f):
+        fn(7)
+    line_b = capfd.readouterr().out
+    assert line_a == line_b and line_a.startswith("Step 7 ")
+    compare_output_dirs(str(a), str(b / "data"), 7, profile_first_column=False)
