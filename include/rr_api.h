@@ -142,6 +142,12 @@ rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const 
  * on the solver's stream (CUDA graphs for long runs). */
 rr_status rr_step(rr_solver *s, int nsteps);
 rr_status rr_sync(rr_solver *s);
+/* Whether the solver's work is still in flight: *busy = 1 while enqueued
+ * steps, uploads or readouts have not finished on its stream, 0 once they
+ * have.  Never waits and does not read the watchdog (rr_sync does).  No
+ * counterpart in the reference, whose host loop synchronises every kernel;
+ * a server polls it to advance each resident domain at its own pace. */
+rr_status rr_query(rr_solver *s, int *busy);
 long long rr_get_istep(const rr_solver *s);
 /* the solver's CUDA stream (a cudaStream_t), for callers that order their own
  * work or CUDA events against the solver's; no counterpart in the reference,

@@ -782,6 +782,22 @@ rr_status rr_sync(rr_solver *s) {
     return RR_OK;
 }
 
+rr_status rr_query(rr_solver *s, int *busy) {
+    if (!s || !busy) return fail(RR_ERR_INVALID, "NULL argument");
+    if (set_device(s) != RR_OK) return RR_ERR_CUDA;
+    const cudaError_t e = cudaStreamQuery(s->stream);
+    if (e == cudaSuccess) {
+        *busy = 0;
+        return RR_OK;
+    }
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError(); // not an error: work in flight
+        *busy = 1;
+        return RR_OK;
+    }
+    return fail(RR_ERR_CUDA, "cudaStreamQuery: %s", cudaGetErrorString(e));
+}
+
 rr_status rr_set_wait_limit(rr_solver *s, long long polls) {
     if (!s) return fail(RR_ERR_INVALID, "solver is NULL");
     if (polls > 0xFFFFFFFFll) return fail(RR_ERR_INVALID, "polls = %lld exceeds 2^32-1", polls);

@@ -604,25 +604,39 @@ __device__ __forceinline__ void store_pair(S *const *dst, uint32_t idx, const F2
 // element offset for both nodes together: one 32-bit (16-bit storage) or
 // 64-bit (FP32) load; the c_x = 0 populations take two scalar loads.  The
 // arithmetic is the scalar node's, lane by lane.
-template <class LT, typename S, bool FORCE, class A>
-__device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
-    const Geom &g = a.g;
-    F2 d[LT::Q];
-    static_for<LT::Q>([&](auto ic) {
-        constexpr int i = decltype(ic)::value;
-        const S *p = a.src[i] + idx;
-        if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
-        else d[i] = ld_pair<S>(p);
-    });
-    const F2 Fx(a.F[0]), Fy(a.F[1]), Fz(a.F[2]);
+// the post-stream populations d of the node pair idx, idx + 1 (idx odd): moments,
+// the watchdog, the collision and the stores
+template <class LT, typename S, bool FORCE>
+__device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t idx, S *const *dst, double om1_,
+                                          const double *Fv, int *status, bool sround) {
+    const F2 Fx(Fv[0]), Fy(Fv[1]), Fz(Fv[2]);
     Mom<F2> m = moments<LT>(d);
     F2 ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
     if (!(m.drho.lo() > -0.9f && m.drho.lo() < 9.0f && m.drho.hi() > -0.9f && m.drho.hi() < 9.0f))
-        atomicOr(a.status, 1);
-    collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, F2(a.om1), Fx, Fy, Fz);
-    store_pair<LT, S>(a.dst, idx, d, g.sround != 0, sr_seed(idx, m.drho.lo(), ux.lo()),
-                      sr_seed(idx + 1u, m.drho.hi(), ux.hi()));
+        atomicOr(status, 1);
+    collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, F2(om1_), Fx, Fy, Fz);
+    store_pair<LT, S>(dst, idx, d, sround, sr_seed(idx, m.drho.lo(), ux.lo()), sr_seed(idx + 1u, m.drho.hi(), ux.hi()));
+}
+
+// the populations of the pair x, x + 1 (x odd) streamed in from row, a run
+// of the source values of one population starting at an even element
+template <class LT, typename S, int I>
+__device__ __forceinline__ F2 pull_pair(const S *row, int x) {
+    if constexpr (LT::cx(I) == 0) return F2(ld_dev<float>(row + x), ld_dev<float>(row + x + 1));
+    else return ld_pair<S>(row + (x - LT::cx(I)));
+}
+
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
+    F2 d[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        const S *p = a.src[i] + idx; // the upstream value of node idx
+        if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
+        else d[i] = ld_pair<S>(p);
+    });
+    pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
 }
 
 // one work item (one warp) of the tile step; A is TileArgs wherever it lives

@@ -26,10 +26,8 @@
 namespace rr {
 
 // a * b + c with one rounding, for every compute type of the node arithmetic
-// (the packed FP32 pair of rr_pair.cuh has its own overload).  The FP32
-// kernels are compiled without automatic multiply-add contraction, so that a
-// node computed alone and a node computed in a packed pair go through the
-// same roundings; the products that should fuse say so here.
+// (the packed FP32 pair of rr_pair.cuh has its own overload): the products
+// that should fuse say so, rather than leaving it to contraction.
 __host__ __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
 __host__ __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
 

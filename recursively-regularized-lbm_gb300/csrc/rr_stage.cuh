@@ -38,7 +38,8 @@ struct StageArgs {
     uint32_t nblocks;     // blocks of up to R interior rows
     uint32_t rows;        // R
     uint32_t yblocks;     // blocks per z plane
-    FastDiv div_yblocks, div_nxi; // div_nxi: nodes per row in the main loop (nx, or nx - 2 with x walls)
+    FastDiv div_yblocks, div_nxi; // div_nxi: work units per row in the main loop (node pairs with 16/32-bit
+                                  // storage; else nodes: nx, or nx - 2 with x walls)
     uint32_t stages;      // S (2 .. STAGE_MAX)
     uint32_t stage_elems; // Q R nx
     double om1;
@@ -107,8 +108,13 @@ constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
 // stage (empty barrier, one arrive per warp), then issues the block's bulk
 // copies onto the stage's full barrier.  The compute warps wait on the full
 // barrier, compute, and release the stage; no barrier over the whole CTA.
+// resident CTAs per SM: the packed-pair compute of 16/32-bit storage keeps
+// two nodes live per thread (2 CTAs, up to 113 registers); FP64 at 3
+template <typename S> constexpr int stage_min_blocks() { return sizeof(S) <= 4 ? 2 : 3; }
+
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(STAGE_THREADS, stage_min_blocks<S>())
+    stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(stage_smem);  // [STAGE_MAX]
@@ -196,6 +202,68 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
         return;
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
+    // 16- and 32-bit storage: the x in [1, nx-2] of a row as packed pairs
+    // (1 + 2p, 2 + 2p) read from the stage (a population's row starts at an
+    // even element: nx is even), x = 0 and x = nx-1 one node per thread
+    constexpr bool PAIR = sizeof(S) <= 4;
+    // one node (r, x) of the block: the stage's row r, a periodic x wrapping
+    // inside the row, an x wall through the gathered bounce-back sources
+    auto node = [&](const S *st, const S *wb, int z, int y0, int r, int x) {
+        const int y = y0 + r;
+        const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
+        const S *row = st + (size_t)r * nx;
+        T d[LT::Q];
+        if (x >= 1 && x <= nx - 2) {
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+            });
+        } else if (!xwall) {
+            // periodic x: the upstream node of an x-face node wraps inside the row
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                int xs = x - LT::cx(i);
+                xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
+                d[i] = ld_dev<T>(row + (size_t)i * R * nx + xs);
+            });
+        } else {
+            // an x wall: the entering populations bounce back from this
+            // node's own post-collision values (gathered into the stage by
+            // the producer), then the face's closure
+            auto wallnode = [&](auto fc) {
+                constexpr int F = decltype(fc)::value;
+                constexpr uint32_t M = entering_mask<LT, F>();
+                const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    if constexpr (((M >> i) & 1u) != 0) {
+                        const T v = ld_dev<T>(wb + ((size_t)F * LT::Q + i) * R + r);
+                        d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+                    } else {
+                        d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+                    }
+                });
+                if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
+            };
+            if (x == 0) wallnode(std::integral_constant<int, 0>{});
+            else wallnode(std::integral_constant<int, 1>{});
+        }
+        Mom<T> m = moments<LT>(d);
+        T ux, uy, uz;
+        velocity(m, Fx, Fy, Fz, ux, uy, uz);
+        if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+        collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+        if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+            if (g.sround) {
+                store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
+                return;
+            }
+        }
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            st_dev<T>(a.dst[i] + idx, d[i]);
+        });
+    };
     for (uint32_t k = 0; k < mine; k++) {
         if (!mbar_wait(&full[k % NS], (k / NS) & 1u, a.wait_limit)) {
             if ((threadIdx.x & 31u) == 0) atomicOr(a.status, WATCH_STAGE_WAIT);
@@ -205,78 +273,37 @@ __global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_co
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
         const S *wb = wall + (size_t)(k % NS) * wall_elems;
-        // the main loop takes every node of the block's rows, or with x walls
-        // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
-        const int nxi = xwall ? nx - 2 : nx;
+        // the main loop: node pairs (or nodes) of the block's rows; the x = 0
+        // and x = nx-1 nodes of the pair layout, or the x-wall nodes, go to
+        // two warps of their own (x = 0, x = nx - 1) after it
+        const int nxi = PAIR ? (nx - 2) / 2 : (xwall ? nx - 2 : nx);
         const int nmain = rows * nxi;
-        const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
-        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nwall;
+        const int nends = (PAIR || xwall) ? 2 * 32 : 0;
+        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nends;
         for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
-            int r, x;
             if (t < nmain) {
-                r = (int)fdiv((uint32_t)t, a.div_nxi);
-                x = (xwall ? 1 : 0) + t - r * nxi;
-            } else {
-                const int w = t - (total - nwall);
-                if (w < 0) continue;        // padding of the main loop's last round
-                r = w & 31;
-                if (r >= rows) continue;
-                x = w < 32 ? 0 : nx - 1;
-            }
-            const int y = y0 + r;
-            const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
-            const S *row = st + (size_t)r * nx;
-            T d[LT::Q];
-            if (x >= 1 && x <= nx - 2) {
-                static_for<LT::Q>([&](auto ic) {
-                    constexpr int i = decltype(ic)::value;
-                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
-                });
-            } else if (!xwall) {
-                // periodic x: the upstream node of an x-face node wraps inside the row
-                static_for<LT::Q>([&](auto ic) {
-                    constexpr int i = decltype(ic)::value;
-                    int xs = x - LT::cx(i);
-                    xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
-                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + xs);
-                });
-            } else {
-                // an x wall: the entering populations bounce back from this
-                // node's own post-collision values (gathered into the stage by
-                // the producer), then the face's closure
-                auto wallnode = [&](auto fc) {
-                    constexpr int F = decltype(fc)::value;
-                    constexpr uint32_t M = entering_mask<LT, F>();
-                    const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
+                const int r = (int)fdiv((uint32_t)t, a.div_nxi);
+                if constexpr (PAIR) {
+                    const int x = 1 + 2 * (t - r * nxi);
+                    const S *row = st + (size_t)r * nx;
+                    F2 d[LT::Q];
                     static_for<LT::Q>([&](auto ic) {
                         constexpr int i = decltype(ic)::value;
-                        if constexpr (((M >> i) & 1u) != 0) {
-                            const T v = ld_dev<T>(wb + ((size_t)F * LT::Q + i) * R + r);
-                            d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
-                        } else {
-                            d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
-                        }
+                        d[i] = pull_pair<LT, S, i>(row + (size_t)i * R * nx, x);
                     });
-                    if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
-                };
-                if (x == 0) wallnode(std::integral_constant<int, 0>{});
-                else wallnode(std::integral_constant<int, 1>{});
-            }
-            Mom<T> m = moments<LT>(d);
-            T ux, uy, uz;
-            velocity(m, Fx, Fy, Fz, ux, uy, uz);
-            if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
-            collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
-            if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
-                if (g.sround) {
-                    store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
-                    continue;
+                    const uint32_t idx =
+                        ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx + (uint32_t)x;
+                    pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, g.sround != 0);
+                } else {
+                    node(st, wb, z, y0, r, (xwall ? 1 : 0) + t - r * nxi);
                 }
+            } else {
+                const int w = t - (total - nends);
+                if (w < 0) continue; // padding of the main loop's last round
+                const int r = w & 31;
+                if (r >= rows) continue;
+                node(st, wb, z, y0, r, w < 32 ? 0 : nx - 1);
             }
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                st_dev<T>(a.dst[i] + idx, d[i]);
-            });
         }
         // this warp is done with stage k % NS
         __syncwarp();

@@ -70,6 +70,7 @@ def lib():
             "rr_init_state": ([vp, vp, vp, vp, vp, vp, ctypes.c_int], ctypes.c_int),
             "rr_step": ([vp, ctypes.c_int], ctypes.c_int),
             "rr_sync": ([vp], ctypes.c_int),
+            "rr_query": ([vp, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
             "rr_get_istep": ([vp], ctypes.c_longlong),
             "rr_get_stream": ([vp], ctypes.c_void_p),
             "rr_macro": ([vp, vp, vp, vp, vp, vp, ctypes.c_int], ctypes.c_int),
@@ -220,6 +221,12 @@ class Solver:
 
     def sync(self):
         _check(lib().rr_sync(self._h))
+
+    def busy(self):
+        """work still in flight on the solver's stream (does not wait)"""
+        b = ctypes.c_int(0)
+        _check(lib().rr_query(self._h, ctypes.byref(b)))
+        return bool(b.value)
 
     @property
     def istep(self):

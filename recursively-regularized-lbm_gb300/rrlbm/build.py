@@ -18,11 +18,7 @@ SOURCES = ["rr_inst_f64.cu", "rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.c
            "rr_aux.cu", "rr_api.cu", "rr_batch.cu", "rr_noalloc.cu"]
 HEADERS = ["rr_lattice.cuh", "rr_node.cuh", "rr_node27.cuh", "rr_kernels.cuh", "rr_les.cuh", "rr_dispatch.h",
            "rr_aux.h", "rr_inst.inc", "rr_internal.h", "rr_stage.cuh", "rr_fdbc.cuh", "rr_pair.cuh"]
-# The FP32-arithmetic translation units (FP32, FP16 and BF16 storage) take no
-# automatic multiply-add contraction: a node computed alone and a node
-# computed in a packed FP32 pair must round identically, and the products that
-# should fuse are written as fma_ in the node arithmetic.
-NO_CONTRACT = {"rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.cu"}
+
 
 
 def _stale(target, deps):
@@ -41,8 +37,7 @@ def build(verbose=False, force=False):
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src.replace(".cu", ".o"))
         if force or _stale(o, [s] + hdrs):
-            extra = ["-fmad=false"] if src in NO_CONTRACT else []
-            jobs.append([NVCC] + ARCH + FLAGS + extra + ["-c", s, "-o", o])
+            jobs.append([NVCC] + ARCH + FLAGS + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -2,19 +2,21 @@
 
 Requests (workloads.Domain: kind, size, step count, storage) arrive over
 time.  The server keeps every admitted domain's state resident on the
-device, admits queued requests in arrival order as soon as the HBM budget
-and the slot limit allow, and advances all resident domains together in
-chunks of steps (one rr_batch_step per chunk).  A chunk ends when the
-first resident domain reaches its step count (or after max_chunk steps, so
-that arrivals never wait longer than one chunk to join); finished domains
-hand their result to on_result and leave, freeing their memory for the
-queue.  Each domain's arithmetic is the same as when it runs alone.
+device and admits queued requests in arrival order as soon as the HBM budget
+and the slot limit allow.  Each resident domain advances on its own CUDA
+stream in chunks of steps; the GPU runs the chunks of all resident domains
+concurrently, and the host never waits for the whole set: it polls each
+domain's stream, enqueues the next chunk of a domain whose chunk has
+finished (so a small solve is never held back by a large one), hands a
+finished domain's result to on_result and frees its memory for the queue.
+Admission (the upload of a new domain's start state, asynchronous on its
+stream) runs while the other domains' chunks are on the GPU.  Each domain's
+arithmetic is the same as when it runs alone.
 
 The device side is a backend object (GpuBackend here; tests substitute a
 host-only fake), so the scheduling logic runs and is tested without a GPU.
 """
 import collections
-import re
 import time
 from dataclasses import dataclass
 
@@ -45,22 +47,26 @@ class Record:
         return self.done - self.arrival
 
 
+class _Member:
+    """a resident domain: its solver and the start fields its asynchronous
+    upload still reads"""
+
+    def __init__(self, solver, keep):
+        self.solver = solver
+        self.keep = keep
+
+
 class GpuBackend:
-    """Resident domains as rr_solver members of one rr_batch."""
+    """Resident domains as rr_solver objects, each on its own stream."""
 
     READOUT_BYTES_PER_NODE = 40  # FP64 rho, u, tau_t scratch a readout allocates
 
-    def __init__(self, device=0, mode=1, chains=16):
-        """mode 1 (default): the members' own launches fanned over `chains`
-        parallel graph branches; mode 0: one persistent batch kernel per step
-        (rr_batch_set_mode)"""
+    def __init__(self, device=0):
         import rrlbm
 
         self._rr = rrlbm
         self.device = device
-        self.batch = rrlbm.Batch(device)
-        self.batch.set_mode(mode, chains)
-        self.members = []  # handles in order of addition (the batch's member order)
+        self.members = []
 
     def bytes_for(self, d):
         from .workloads import params_of
@@ -68,45 +74,51 @@ class GpuBackend:
         return self._rr.bytes_for(params_of(d)) + self.READOUT_BYTES_PER_NODE * d.nodes
 
     def start(self, d):
+        """create the domain and enqueue its state upload (asynchronous)"""
         from .workloads import macros_on_device, params_of
 
         s = self._rr.Solver(params_of(d))
-        rho, ux, uy, uz = macros_on_device(d, f"cuda:{self.device}")
-        s.init_state(rho, ux, uy, uz)
-        self.batch.add(s)  # waits for the solver's upload: the fields may go
-        self.members.append(s)
-        return s
+        fields = macros_on_device(d, f"cuda:{self.device}")
+        s.init_state(*fields)
+        h = _Member(s, fields)
+        self.members.append(h)
+        return h
 
-    def step(self, n):
-        self.batch.step(n)
+    def advance(self, h, n):
+        """enqueue n steps of h on its stream"""
+        h.solver.step(n)
 
-    def sync(self):
-        """None, or the index (order of addition) of a member whose watchdog fired"""
+    def ready(self, h):
+        """h's enqueued work has finished (does not wait)"""
+        if h.solver.busy():
+            return False
+        h.keep = None  # the upload has read the start fields
+        return True
+
+    def healthy(self, h):
+        """h's watchdog has not fired (call once h is ready)"""
         try:
-            self.batch.sync()
-            return None
+            h.solver.sync()
+            return True
         except self._rr.RRError as e:
             if e.code != 5:
                 raise
-            m = re.search(r"member (\d+)", str(e))
-            return int(m.group(1)) if m else 0
+            return False
 
     def finish(self, h, on_result=None):
-        res = on_result(h) if on_result else None
-        self.batch.remove(h)
+        res = on_result(h.solver) if on_result else None
         self.members.remove(h)
-        h.close()
+        h.solver.close()
         return res
 
     def close(self):
         for h in list(self.members):
             self.finish(h)
-        self.batch.close()
 
 
 class Server:
-    def __init__(self, backend, budget_bytes, max_chunk=500, max_active=None, on_result=None,
-                 clock=time.perf_counter, sleep=time.sleep):
+    def __init__(self, backend, budget_bytes, max_chunk=2000, max_active=None, on_result=None,
+                 clock=time.perf_counter, sleep=time.sleep, poll_s=2e-4):
         self.backend = backend
         self.budget = int(budget_bytes)
         self.max_chunk = int(max_chunk)
@@ -114,6 +126,7 @@ class Server:
         self.on_result = on_result
         self.clock = clock
         self.sleep = sleep
+        self.poll_s = poll_s
         self.chunks = 0
         self.peak_bytes = 0
         self.peak_active = 0
@@ -124,16 +137,25 @@ class Server:
         reqs = sorted(requests, key=lambda r: r.arrival)
         recs = {r.rid: Record(r.rid, r.arrival, r.nodes, r.steps) for r in reqs}
         queue = collections.deque()
-        active = []  # [request, handle, bytes, remaining steps]
+        active = []  # [request, handle, bytes, steps not yet enqueued, steps of the chunk in flight]
         used = 0
         i = 0
         t0 = self.clock()
+
+        def enqueue(a):
+            n = min(self.max_chunk, a[3])
+            self.backend.advance(a[1], n)
+            a[3] -= n
+            a[4] = n
+            self.chunks += 1
+
         while i < len(reqs) or queue or active:
             now = self.clock() - t0
             while i < len(reqs) and reqs[i].arrival <= now:
                 queue.append(reqs[i])
                 i += 1
-            # admission in arrival order, by memory budget and slot limit
+            # admission in arrival order, by memory budget and slot limit; a
+            # new domain's upload and first chunk go in behind the others'
             while queue and (self.max_active is None or len(active) < self.max_active):
                 r = queue[0]
                 b = self.backend.bytes_for(r)
@@ -147,37 +169,40 @@ class Server:
                 queue.popleft()
                 h = self.backend.start(r)
                 used += b
-                active.append([r, h, b, r.steps])
+                a = [r, h, b, r.steps, 0]
+                active.append(a)
                 recs[r.rid].admit = self.clock() - t0
+                enqueue(a)
             self.peak_bytes = max(self.peak_bytes, used)
             self.peak_active = max(self.peak_active, len(active))
-            if not active:
-                if i < len(reqs):
-                    wait = reqs[i].arrival - (self.clock() - t0)
-                    if wait > 0:
-                        self.sleep(wait)
+            # completions: per domain, without waiting for the others
+            progressed = False
+            for a in list(active):
+                if not self.backend.ready(a[1]):
+                    continue
+                progressed = True
+                rec = recs[a[0].rid]
+                if not self.backend.healthy(a[1]):
+                    # the domain that blew up leaves with an error; the others go on
+                    self.backend.finish(a[1])
+                    rec.error = "watchdog: density out of range or NaN"
+                elif a[3] > 0:
+                    enqueue(a)
+                    continue
+                else:
+                    rec.result = self.backend.finish(a[1], self.on_result)
+                rec.done = self.clock() - t0
+                used -= a[2]
+                active.remove(a)
+            if progressed:
                 continue
-            chunk = min(self.max_chunk, min(a[3] for a in active))
-            self.backend.step(chunk)
-            self.chunks += 1
-            for a in active:
-                a[3] -= chunk
-            bad = self.backend.sync()
-            now = self.clock() - t0
-            while bad is not None:
-                # the member that blew up leaves with an error; the others go on
-                a = next(x for x in active if x[1] is self.backend.members[bad])
-                self.backend.finish(a[1])
-                recs[a[0].rid].error = "watchdog: density out of range or NaN"
-                recs[a[0].rid].done = now
-                used -= a[2]
-                active.remove(a)
-                bad = self.backend.sync()
-            for a in [x for x in active if x[3] == 0]:
-                recs[a[0].rid].result = self.backend.finish(a[1], self.on_result)
-                recs[a[0].rid].done = self.clock() - t0
-                used -= a[2]
-                active.remove(a)
+            # nothing finished: wait a poll interval, or until the next arrival
+            # when nothing is resident
+            wait = self.poll_s
+            if not active and i < len(reqs):
+                wait = max(reqs[i].arrival - (self.clock() - t0), 0.0)
+            if wait > 0:
+                self.sleep(wait)
         return [recs[r.rid] for r in requests]
 
 

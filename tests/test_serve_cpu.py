@@ -19,7 +19,9 @@ class FakeClock:
 
 
 class FakeBackend:
-    """Resident domains advance at a fixed aggregate rate (nodes*steps/s)."""
+    """Resident domains on their own 'streams': a chunk of n steps of a domain
+    takes n * nodes / (rate / resident domains) seconds of the fake clock
+    (the device's aggregate rate, shared)."""
 
     def __init__(self, clock, rate=1e9, bad=()):
         self.clock = clock
@@ -34,23 +36,27 @@ class FakeBackend:
         return 100 * d.nodes
 
     def start(self, d):
-        h = {"d": d, "steps": 0}
+        h = {"d": d, "steps": 0, "pending": 0, "until": self.clock.t}
         self.members.append(h)
         self.starts.append(d.rid)
         self.used += self.bytes_for(d)
         self.peak = max(self.peak, self.used)
         return h
 
-    def step(self, n):
-        self.clock.t += n * sum(h["d"].nodes for h in self.members) / self.rate
-        for h in self.members:
-            h["steps"] += n
+    def advance(self, h, n):
+        share = self.rate / max(1, len(self.members))
+        h["until"] = max(h["until"], self.clock.t) + n * h["d"].nodes / share
+        h["pending"] += n
 
-    def sync(self):
-        for k, h in enumerate(self.members):
-            if h["d"].rid in self.bad:
-                return k
-        return None
+    def ready(self, h):
+        if self.clock.t < h["until"]:
+            return False
+        h["steps"] += h["pending"]
+        h["pending"] = 0
+        return True
+
+    def healthy(self, h):
+        return h["d"].rid not in self.bad
 
     def finish(self, h, on_result=None):
         res = on_result(h) if on_result else None
