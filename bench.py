@@ -25,12 +25,14 @@ Line fields (one JSON line on rank 0):
              CUDA graphs, against the same domains stepped one at a time
              (each domain's own rr_step, synchronised) and on concurrent
              per-domain streams; aggregate MLUPS over a fixed step count.
-  serving    the served form: a seeded Poisson stream of Taylor-Green, cavity
-             and WALE channel solves (32^3-192^3, 1k-20k steps, FP16/FP32)
-             through the continuous-batching server under an 80 GB budget,
-             against a one-at-a-time server; solves/s, p50/p99 latency
-             (queueing and device parts) and each sampled solve's velocity
-             error against its FP64 rerun.
+  serving    the served form: seeded Poisson streams of Taylor-Green, cavity
+             and WALE channel solves (the mixed stream: 32^3-192^3, 1k-20k
+             steps at 200 req/s; the small-solve stream: 32^3-64^3, 1k-4k
+             steps at 400 req/s) through the continuous-batching server under
+             an 80 GB budget, against a one-at-a-time server; solves/s,
+             p50/p99 latency (overall, per size class, queueing and device
+             parts) and each sampled solve's velocity error against its FP64
+             rerun.
 --impl reference runs that CPU implementation alone as the reference arm.
 Multi-GPU (torchrun, N > 1): independent replicas, one domain per GPU.
 """
@@ -468,15 +470,56 @@ def run_batch(args):
     return out
 
 
+SERVE_STREAMS = {
+    # the served workload: Taylor-Green / cavity / WALE channel, n^3 with n in
+    # [32, 192] and steps in [1000, 20000] log-uniform, Poisson 200 req/s
+    "mixed": dict(rate=200.0, seed=5, sizes=(32, 192), steps=(1000, 20000), scale=1),
+    # small solves dominate: n in [32, 64], steps in [1000, 4000], Poisson
+    # 400 req/s, five times the requests (a rate one domain at a time cannot
+    # keep up with: its small grids leave the GPU mostly idle)
+    "small": dict(rate=400.0, seed=9, sizes=(32, 64), steps=(1000, 4000), scale=5),
+}
+
+
+def serve_stream(name, count):
+    from rrlbm import workloads
+    c = SERVE_STREAMS[name]
+    return workloads.request_stream(count * c["scale"], rate=c["rate"], seed=c["seed"], sizes=c["sizes"],
+                                    steps=c["steps"])
+
+
 def run_serve(args):
     """The served form: continuous batching against one-at-a-time serving on
-    the same seeded request stream, and sampled errors against FP64 reruns."""
+    the same seeded request streams, and sampled errors against FP64 reruns."""
     import numpy as np
     from rrlbm import serve, workloads
 
-    reqs = workloads.request_stream(args.serve_requests, rate=200.0, seed=5)
     budget = 80e9
-    # the solves whose FP64 rerun is affordable: the smallest by work, up to ~2e10 updates
+    out = {"budget_bytes": budget}
+    for name in SERVE_STREAMS:
+        reqs = serve_stream(name, args.serve_requests)
+        c = SERVE_STREAMS[name]
+        o = {"requests": len(reqs), "rate_per_s": c["rate"], "seed": c["seed"],
+             "mix": f"Poisson arrivals; Taylor-Green / cavity / WALE channel; n^3 with n in "
+                    f"[{c['sizes'][0]}, {c['sizes'][1]}] and steps in [{c['steps'][0]}, {c['steps'][1]}] "
+                    f"log-uniform; FP16 or FP32 storage, FP32 compute"}
+        for mode, slots in (("batched", None), ("one_at_a_time", 1)):
+            be = serve.GpuBackend()
+            # each solve's result: its domain means (rr_diag), read before it leaves
+            srv = serve.Server(be, budget, max_active=slots, on_result=lambda s: s.diag())
+            recs = srv.run(reqs)
+            be.close()
+            st = serve.summarize(recs)
+            st["chunks"] = srv.chunks
+            st["peak_resident"] = srv.peak_active
+            st["peak_bytes"] = srv.peak_bytes
+            o[mode] = st
+        o["speedup_solves_per_s"] = o["batched"]["solves_per_s"] / o["one_at_a_time"]["solves_per_s"]
+        out[name] = o
+    # errors against FP64 reruns, sampled solves of the mixed stream (served
+    # arithmetic = alone arithmetic, bit for bit, so the served result is the
+    # alone run): the smallest by work, up to ~2e10 updates
+    reqs = serve_stream("mixed", args.serve_requests)
     order = sorted(reqs, key=lambda d: d.nodes * d.steps)
     sample, work = set(), 0.0
     for d in order:
@@ -484,22 +527,6 @@ def run_serve(args):
             break
         sample.add(d.rid)
         work += d.nodes * d.steps
-    out = {"requests": len(reqs), "rate_per_s": 200.0, "budget_bytes": budget, "seed": 5,
-           "mix": "Poisson arrivals; Taylor-Green / cavity / WALE channel; n^3 with n in [32, 192] and "
-                  "steps in [1000, 20000] log-uniform; FP16 or FP32 storage, FP32 compute"}
-    for mode, slots in (("batched", None), ("one_at_a_time", 1)):
-        be = serve.GpuBackend()
-        # each solve's result: its domain means (rr_diag), read before it leaves
-        srv = serve.Server(be, budget, max_chunk=500, max_active=slots, on_result=lambda s: s.diag())
-        recs = srv.run(reqs)
-        be.close()
-        st = serve.summarize(recs)
-        st["chunks"] = srv.chunks
-        st["peak_resident"] = srv.peak_active
-        st["peak_bytes"] = srv.peak_bytes
-        out[mode] = st
-    # errors against FP64 reruns, sampled solves (served arithmetic = alone arithmetic,
-    # bit for bit, so the served result is the alone run)
     errs = []
     for d in reqs:
         if d.rid not in sample:
@@ -515,7 +542,6 @@ def run_serve(args):
         errs.append({"rid": d.rid, "kind": d.kind, "n": d.n, "steps": d.steps, "storage": d.storage,
                      "max_err_rel_u": e_max, "l2_rel": (num / den) ** 0.5 if den > 0 else None})
     out["fp64_rerun_errors"] = errs
-    out["speedup_solves_per_s"] = out["batched"]["solves_per_s"] / out["one_at_a_time"]["solves_per_s"]
     return out
 
 

@@ -231,4 +231,19 @@ def summarize(records):
         "queue_p99_s": pct(q, 99),
         "device_p50_s": pct(dev, 50),
         "device_p99_s": pct(dev, 99),
+        "by_size": by_size(ok),
     }
+
+
+SIZE_CLASSES = ((0, 48 ** 3, "n <= 48"), (48 ** 3, 96 ** 3, "48 < n <= 96"), (96 ** 3, float("inf"), "n > 96"))
+
+
+def by_size(records):
+    """latency percentiles per cube-size class (n^3 nodes)"""
+    out = {}
+    for lo, hi, name in SIZE_CLASSES:
+        sel = [r.latency for r in records if lo < r.nodes <= hi]
+        if sel:
+            out[name] = {"count": len(sel), "latency_p50_s": float(np.percentile(sel, 50)),
+                         "latency_p99_s": float(np.percentile(sel, 99))}
+    return out
