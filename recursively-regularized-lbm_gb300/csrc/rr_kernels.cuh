@@ -639,23 +639,16 @@ __device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
     pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
 }
 
-// one work item (one warp) of the tile step; A is TileArgs wherever it lives
-// (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
-// DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
-// applies the walls and writes the velocity field; MODE 2 streams again,
-// takes tau_t from the 7-point stencil of that field and collides.
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
-__device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
-    // the packed-pair form: 16- and 32-bit storage, the DNS step with a
-    // uniform force and the RR collision (the host sets a.pairs only then,
-    // and only for an even nx)
-    constexpr bool PAIRABLE = sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
-    if (item >= a.nitems) return;
-    bool pair = false;
+// The node(s) a lane of work item `item` takes: false if none.  The slow
+// items go first so that they overlap the bulk instead of forming a tail: the
+// edge items, then the rows of the last z plane (the row order is rotated by
+// one plane).  pair: the lane takes the node pair (x, x + 1).
+template <bool PAIRABLE, class A>
+__device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t lane, uint32_t &row, int &x,
+                                            int &y, int &z, bool &fast, bool &pair) {
+    pair = false;
+    if (item >= a.nitems) return false;
     const Geom &g = a.g;
-    uint32_t row;
-    int x, y, z;
-    bool fast;
     // the slow items go first so that they overlap the bulk instead of
     // forming a tail: the edge items, then the rows of the last z plane (the
     // row order is rotated by one plane)
@@ -669,12 +662,12 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
             const uint32_t rl = fdiv(sub, a.div_segs);
             row = grp * a.rows_group + rl;
             const uint32_t col = (sub - rl * a.segs) * 32u + lane;
-            if constexpr (PAIRABLE) pair = a.pairs != 0;
+            pair = PAIRABLE && a.pairs != 0;
             // pairs (1 + 2 col, 2 + 2 col): an even nx has an even number of
             // interior nodes, so the pairs cover x in [1, nx-2] exactly
             x = 1 + (int)(pair ? 2u * col : col);
             fast = true;
-            if (x > g.nx - 2) return;
+            if (x > g.nx - 2) return false;
         } else {
             // the x = 0 nodes of the group's rows, 32 per item, then the
             // x = nx-1 nodes: whole CTAs of these slower items
@@ -685,18 +678,18 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
             fast = false;
             xface = true;
         }
-        if (row >= a.nrows) return;
+        if (row >= a.nrows) return false;
         row += a.rot;
         if (row >= a.nrows) row -= a.nrows;
         z = (int)fdiv(row, a.div_ny);
         y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
         const bool yzw = ((a.yzwall & 1u) && y == 0) || ((a.yzwall & 2u) && y == g.ny - 1) ||
                          ((a.yzwall & 4u) && z == 0) || ((a.yzwall & 8u) && z == g.nz - 1);
-        if (xface && yzw) return; // an edge node: handled by the edge items
+        if (xface && yzw) return false; // an edge node: handled by the edge items
         fast = fast && y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2;
     } else {
         const uint32_t e = item * 32u + lane;
-        if (e >= a.nedges) return;
+        if (e >= a.nedges) return false;
         const uint32_t nidx = a.edges[e];
         row = fdiv(nidx, a.div_nx);
         x = (int)(nidx - row * (uint32_t)g.nx);
@@ -704,9 +697,27 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
         y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
         fast = false;
     }
+    return true;
+}
+
+// one work item (one warp) of the tile step; A is TileArgs wherever it lives
+// (kernel parameters for one domain, shared memory for a batch).  MODE 0: the
+// DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
+// applies the walls and writes the velocity field; MODE 2 streams again,
+// takes tau_t from the 7-point stencil of that field and collides.
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
+__device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
+    // the packed-pair form: 16- and 32-bit storage, the DNS step with a
+    // uniform force and the RR collision (the host sets a.pairs only then,
+    // and only for an even nx)
+    constexpr bool PAIRABLE = sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
+    uint32_t row;
+    int x, y, z;
+    bool fast, pair;
+    if (!tile_decode<PAIRABLE>(a, item, lane, row, x, y, z, fast, pair)) return;
     if constexpr (PAIRABLE) {
         if (pair && fast) {
-            pair_node<LT, S, FORCE>(a, row * (uint32_t)g.nx + (uint32_t)x);
+            pair_node<LT, S, FORCE>(a, row * (uint32_t)a.g.nx + (uint32_t)x);
             return;
         }
     }
@@ -717,9 +728,84 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     for (int k = 0; k < nn; k++) tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x + k, y, z, fast);
 }
 
+// The 16-bit populations of the node pair idx, idx + 1 (idx odd) as they are
+// stored: one word (two halves) per population, the c_x = 0 ones assembled
+// from two 16-bit loads
+template <class LT, typename S, class A>
+__device__ __forceinline__ void pair_load_raw(const A &a, uint32_t idx, uint32_t (&w)[LT::Q]) {
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        const S *p = a.src[i] + idx;
+        if constexpr (LT::cx(i) == 0) {
+            const uint32_t lo = *reinterpret_cast<const unsigned short *>(p);
+            const uint32_t hi = *reinterpret_cast<const unsigned short *>(p + 1);
+            w[i] = __byte_perm(lo, hi, 0x5410);
+        } else {
+            w[i] = *reinterpret_cast<const uint32_t *>(p);
+        }
+    });
+}
+
+template <typename S> __device__ __forceinline__ F2 raw_pair(uint32_t w) {
+    if constexpr (std::is_same<S, __half>::value)
+        return F2(__half22float2(*reinterpret_cast<const __half2 *>(&w)));
+    else
+        return F2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w)));
+}
+
+// Two consecutive work items in one warp (16-bit storage, the DNS step).
+// When both are row items of fast rows, the warp issues the loads of both
+// node pairs before it computes either, so each warp keeps twice the loads in
+// flight: the stored 16-bit words stay packed (one register per population
+// and pair) until their pair is computed.  Any other items run one after the
+// other.  The arithmetic of every node is that of tile_item.
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ void tile_item2(const A &a, uint32_t item0, uint32_t lane) {
+    uint32_t r0, r1;
+    int x0, y0, z0, x1, y1, z1;
+    bool f0, p0, f1, p1;
+    const bool v0 = tile_decode<true>(a, item0, lane, r0, x0, y0, z0, f0, p0);
+    const bool v1 = tile_decode<true>(a, item0 + 1, lane, r1, x1, y1, z1, f1, p1);
+    const bool both = __all_sync(0xffffffffu, (!v0 || (f0 && p0)) && (!v1 || (f1 && p1)));
+    if (both) {
+        const uint32_t nx = (uint32_t)a.g.nx;
+        const uint32_t i0 = r0 * nx + (uint32_t)x0, i1 = r1 * nx + (uint32_t)x1;
+        uint32_t w0[LT::Q], w1[LT::Q];
+        if (v0) pair_load_raw<LT, S>(a, i0, w0);
+        if (v1) pair_load_raw<LT, S>(a, i1, w1);
+        if (v0) {
+            F2 d[LT::Q];
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                d[i] = raw_pair<S>(w0[i]);
+            });
+            pair_core<LT, S, FORCE>(d, i0, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
+        }
+        if (v1) {
+            F2 d[LT::Q];
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                d[i] = raw_pair<S>(w1[i]);
+            });
+            pair_core<LT, S, FORCE>(d, i1, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
+        }
+        return;
+    }
+#pragma unroll 1
+    for (uint32_t k = 0; k < 2; k++) tile_item<LT, S, FORCE>(a, item0 + k, lane);
+}
+
+// the tile step's warps take two work items each (tile_item2): 16-bit
+// storage, the DNS step with a uniform force and the RR collision
+template <typename S, int MODE, bool FIELD, bool BGK> __host__ __device__ constexpr bool tile_two_items() {
+    return sizeof(S) == 2 && MODE == 0 && !FIELD && !BGK;
+}
+
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
 __global__ void __launch_bounds__(256, tile_min_blocks<S, MODE, FIELD, BGK>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if constexpr (tile_two_items<S, MODE, FIELD, BGK>()) tile_item2<LT, S, FORCE>(a, 2u * w, threadIdx.x & 31u);
+    else tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, w, threadIdx.x & 31u);
 }
 
 

@@ -2,7 +2,7 @@
 //
 // The node arithmetic of rr_node.cuh is written once over its compute type
 // T.  F2 is a pair of FP32 values (two x-adjacent nodes) whose operations map
-// to the packed FP32x2 instructions of sm_100-family GPUs (add/mul/fma
+// to the packed FP32x2 instructions of sm_100-family GPUs (add/sub/mul/fma
 // .rn.f32x2): one instruction does the work of two scalar FP32 instructions,
 // which halves the issue slots the collision takes.  Each lane of an F2
 // operation rounds exactly as the scalar FP32 operation does, and the
@@ -35,9 +35,13 @@ struct F2 {
 __device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
 __device__ __forceinline__ F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
 __device__ __forceinline__ F2 operator-(F2 a) { return F2(make_float2(-a.v.x, -a.v.y)); }
-// a - b as a + (-b), as the scalar subtraction is an addition of the negated
-// operand (the same contraction opportunities for the compiler)
-__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2(__fadd2_rn(a.v, (-b).v)); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+    unsigned long long r;
+    const unsigned long long x = *reinterpret_cast<const unsigned long long *>(&a.v);
+    const unsigned long long y = *reinterpret_cast<const unsigned long long *>(&b.v);
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(x), "l"(y));
+    return F2(*reinterpret_cast<const float2 *>(&r));
+}
 // IEEE division lane by lane (as the scalar FP32 division)
 __device__ __forceinline__ F2 operator/(F2 a, F2 b) {
     return F2(make_float2(__fdiv_rn(a.v.x, b.v.x), __fdiv_rn(a.v.y, b.v.y)));

@@ -12,6 +12,7 @@ through rr_load and continues as the uninterrupted run does (1e-13 on rho and
 f, 1e-12 of the velocity scale on u: the upload re-forms the deviations from
 FP64 populations)."""
 import os
+import re
 
 import numpy as np
 import pytest
@@ -27,8 +28,8 @@ ALL = rrlbm.OUT_DIAG | rrlbm.OUT_FLOW | rrlbm.OUT_PROFILE | rrlbm.OUT_F
 
 
 def _console_numbers(line):
-    parts = line.replace(",", " ").split()
-    return [float(x) for x in parts if any(c in x for c in "e.")]
+    """the four %e numbers of diag_flow's console line"""
+    return [float(x) for x in re.findall(r"[-+]?\d\.\d+e[-+]\d+", line)]
 
 
 @pytest.mark.parametrize("les", [True, False])
