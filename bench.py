@@ -55,6 +55,8 @@ WORKLOADS = {
     "cavity128_f64": dict(kind="cavity", n=128, storage="f64", Re=1000.0, U=0.1),
     "cavity128_bf16": dict(kind="cavity", n=128, storage="bf16", Re=1000.0, U=0.1),
     "channel_les_f16": dict(kind="channel", storage="f16"),
+    "channel_les_f32": dict(kind="channel", storage="f32"),
+    "channel_les_f64": dict(kind="channel", storage="f64"),
     "channel_dns_f16": dict(kind="channel", storage="f16", les=False),
     "channel_fdbc_f16": dict(kind="channel", storage="f16", les=False, fdbc=True),
     "channel_les_fdbc_f16": dict(kind="channel", storage="f16", fdbc=True),

@@ -563,39 +563,40 @@ __device__ __forceinline__ void tile_node(const A &a, uint32_t row, int x, int y
     });
 }
 
-// Stores two x-adjacent nodes' populations (idx: the first node, at an odd
-// element offset, so every store is a 16- or 32-bit scalar store).  With
+// Stores two nodes' populations (ia: the low lane's node, ib the high
+// lane's: x-adjacent nodes at an odd and an even element, or the two x ends
+// of a periodic row; every store is a 16- or 32-bit scalar store).  With
 // stochastic rounding each node draws from its own stream exactly as
 // store_sr_pairs does for a node alone: per population pair (i0, i1) one LCG
 // draw r, folded f = r ^ (r >> 16), whose low half rounds i0 and high half
 // i1; one packed conversion rounds population i of both nodes, the first
 // node's bits in the low half of the random operand, the second's in the high.
 template <class LT, typename S>
-__device__ __forceinline__ void store_pair(S *const *dst, uint32_t idx, const F2 (&d)[LT::Q], bool sround,
-                                           uint32_t sa, uint32_t sb) {
+__device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, uint32_t ib, const F2 (&d)[LT::Q],
+                                           bool sround, uint32_t sa, uint32_t sb) {
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (sround) {
             uint32_t ra = sa, rb = sb;
             auto put = [&](S *p, uint32_t w) {
-                *reinterpret_cast<unsigned short *>(p) = (unsigned short)(w & 0xFFFFu);
-                *reinterpret_cast<unsigned short *>(p + 1) = (unsigned short)(w >> 16);
+                *reinterpret_cast<unsigned short *>(p + ia) = (unsigned short)(w & 0xFFFFu);
+                *reinterpret_cast<unsigned short *>(p + ib) = (unsigned short)(w >> 16);
             };
             static_for<(LT::Q + 1) / 2>([&](auto jc) {
                 constexpr int i0 = 2 * decltype(jc)::value, i1 = i0 + 1;
                 ra = ra * 1664525u + 1013904223u;
                 rb = rb * 1664525u + 1013904223u;
                 const uint32_t fa = ra ^ (ra >> 16), fb = rb ^ (rb >> 16);
-                put(dst[i0] + idx, cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)));
+                put(dst[i0], cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)));
                 if constexpr (i1 < LT::Q)
-                    put(dst[i1] + idx, cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)));
+                    put(dst[i1], cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)));
             });
             return;
         }
     }
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        st_dev<float>(dst[i] + idx, d[i].lo());
-        st_dev<float>(dst[i] + idx + 1, d[i].hi());
+        st_dev<float>(dst[i] + ia, d[i].lo());
+        st_dev<float>(dst[i] + ib, d[i].hi());
     });
 }
 
@@ -604,10 +605,10 @@ __device__ __forceinline__ void store_pair(S *const *dst, uint32_t idx, const F2
 // element offset for both nodes together: one 32-bit (16-bit storage) or
 // 64-bit (FP32) load; the c_x = 0 populations take two scalar loads.  The
 // arithmetic is the scalar node's, lane by lane.
-// the post-stream populations d of the node pair idx, idx + 1 (idx odd): moments,
-// the watchdog, the collision and the stores
+// the post-stream populations d of the node pair ia (low lane), ib (high
+// lane): moments, the watchdog, the collision and the stores
 template <class LT, typename S, bool FORCE>
-__device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t idx, S *const *dst, double om1_,
+__device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, uint32_t ib, S *const *dst, double om1_,
                                           const double *Fv, int *status, bool sround) {
     const F2 Fx(Fv[0]), Fy(Fv[1]), Fz(Fv[2]);
     Mom<F2> m = moments<LT>(d);
@@ -616,7 +617,7 @@ __device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t idx, S *const
     if (!(m.drho.lo() > -0.9f && m.drho.lo() < 9.0f && m.drho.hi() > -0.9f && m.drho.hi() < 9.0f))
         atomicOr(status, 1);
     collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, F2(om1_), Fx, Fy, Fz);
-    store_pair<LT, S>(dst, idx, d, sround, sr_seed(idx, m.drho.lo(), ux.lo()), sr_seed(idx + 1u, m.drho.hi(), ux.hi()));
+    store_pair<LT, S>(dst, ia, ib, d, sround, sr_seed(ia, m.drho.lo(), ux.lo()), sr_seed(ib, m.drho.hi(), ux.hi()));
 }
 
 // the populations of the pair x, x + 1 (x odd) streamed in from row, a run
@@ -625,6 +626,48 @@ template <class LT, typename S, int I>
 __device__ __forceinline__ F2 pull_pair(const S *row, int x) {
     if constexpr (LT::cx(I) == 0) return F2(ld_dev<float>(row + x), ld_dev<float>(row + x + 1));
     else return ld_pair<S>(row + (x - LT::cx(I)));
+}
+
+// The regularized closure (regularize) of a node pair whose two nodes lie on
+// different wall faces: the closure value of every population in CMASK is
+// formed for both lanes, and each lane takes it where its own mask (mlo, mhi)
+// has the population.  Lane by lane this is regularize() of that node.
+template <class LT, bool FORCE, uint32_t CMASK>
+__device__ __forceinline__ void regularize_pair(F2 (&d)[LT::Q], uint32_t mlo, uint32_t mhi, F2 Fx, F2 Fy, F2 Fz) {
+    using T = F2;
+    Mom<T> m = moments<LT>(d);
+    T ux, uy, uz;
+    velocity(m, Fx, Fy, Fz, ux, uy, uz);
+    const T rho = T(1) + m.drho;
+    T n[6];
+    aneq_base(m, rho, ux, uy, uz, n);
+    T Aq[6], Bq[10];
+    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
+    T Fe = T(0);
+    if constexpr (FORCE) {
+        Fe = T(-1.5) * (ux * Fx + uy * Fy + uz * Fz);
+        T C[6];
+        force_correction<LT>(m.drho, Aq, Bq, Fe, Fx, Fy, Fz, C);
+#pragma unroll
+        for (int k = 0; k < 6; k++) n[k] += C[k];
+    }
+    T Bn[10];
+    third_from_second(n, ux, uy, uz, T(1), Bn);
+    const uint32_t mask = mlo | mhi;
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        if constexpr (((CMASK >> i) & 1u) != 0)
+        if ((mask >> i) & 1u) {
+            T Ee = m.drho + even_poly<LT, i>(Aq);
+            T Eo = odd_poly<LT, i>(Bq);
+            T v = Ee + Eo + even_poly<LT, i>(n) + odd_poly<LT, i, T, false>(Bn);
+            if constexpr (FORCE) {
+                T Fo = T(1.5) * (T(LT::cx(i)) * Fx + T(LT::cy(i)) * Fy + T(LT::cz(i)) * Fz);
+                v -= (T(1) + Ee + Eo) * (Fe + Fo);
+            }
+            d[i] = F2(((mlo >> i) & 1u) ? v.lo() : d[i].lo(), ((mhi >> i) & 1u) ? v.hi() : d[i].hi());
+        }
+    });
 }
 
 template <class LT, typename S, bool FORCE, class A>
@@ -636,7 +679,7 @@ __device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
         if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
         else d[i] = ld_pair<S>(p);
     });
-    pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
+    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
 }
 
 // The node(s) a lane of work item `item` takes: false if none.  The slow
@@ -728,84 +771,9 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     for (int k = 0; k < nn; k++) tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x + k, y, z, fast);
 }
 
-// The 16-bit populations of the node pair idx, idx + 1 (idx odd) as they are
-// stored: one word (two halves) per population, the c_x = 0 ones assembled
-// from two 16-bit loads
-template <class LT, typename S, class A>
-__device__ __forceinline__ void pair_load_raw(const A &a, uint32_t idx, uint32_t (&w)[LT::Q]) {
-    static_for<LT::Q>([&](auto ic) {
-        constexpr int i = decltype(ic)::value;
-        const S *p = a.src[i] + idx;
-        if constexpr (LT::cx(i) == 0) {
-            const uint32_t lo = *reinterpret_cast<const unsigned short *>(p);
-            const uint32_t hi = *reinterpret_cast<const unsigned short *>(p + 1);
-            w[i] = __byte_perm(lo, hi, 0x5410);
-        } else {
-            w[i] = *reinterpret_cast<const uint32_t *>(p);
-        }
-    });
-}
-
-template <typename S> __device__ __forceinline__ F2 raw_pair(uint32_t w) {
-    if constexpr (std::is_same<S, __half>::value)
-        return F2(__half22float2(*reinterpret_cast<const __half2 *>(&w)));
-    else
-        return F2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w)));
-}
-
-// Two consecutive work items in one warp (16-bit storage, the DNS step).
-// When both are row items of fast rows, the warp issues the loads of both
-// node pairs before it computes either, so each warp keeps twice the loads in
-// flight: the stored 16-bit words stay packed (one register per population
-// and pair) until their pair is computed.  Any other items run one after the
-// other.  The arithmetic of every node is that of tile_item.
-template <class LT, typename S, bool FORCE, class A>
-__device__ __forceinline__ void tile_item2(const A &a, uint32_t item0, uint32_t lane) {
-    uint32_t r0, r1;
-    int x0, y0, z0, x1, y1, z1;
-    bool f0, p0, f1, p1;
-    const bool v0 = tile_decode<true>(a, item0, lane, r0, x0, y0, z0, f0, p0);
-    const bool v1 = tile_decode<true>(a, item0 + 1, lane, r1, x1, y1, z1, f1, p1);
-    const bool both = __all_sync(0xffffffffu, (!v0 || (f0 && p0)) && (!v1 || (f1 && p1)));
-    if (both) {
-        const uint32_t nx = (uint32_t)a.g.nx;
-        const uint32_t i0 = r0 * nx + (uint32_t)x0, i1 = r1 * nx + (uint32_t)x1;
-        uint32_t w0[LT::Q], w1[LT::Q];
-        if (v0) pair_load_raw<LT, S>(a, i0, w0);
-        if (v1) pair_load_raw<LT, S>(a, i1, w1);
-        if (v0) {
-            F2 d[LT::Q];
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                d[i] = raw_pair<S>(w0[i]);
-            });
-            pair_core<LT, S, FORCE>(d, i0, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
-        }
-        if (v1) {
-            F2 d[LT::Q];
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                d[i] = raw_pair<S>(w1[i]);
-            });
-            pair_core<LT, S, FORCE>(d, i1, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
-        }
-        return;
-    }
-#pragma unroll 1
-    for (uint32_t k = 0; k < 2; k++) tile_item<LT, S, FORCE>(a, item0 + k, lane);
-}
-
-// the tile step's warps take two work items each (tile_item2): 16-bit
-// storage, the DNS step with a uniform force and the RR collision
-template <typename S, int MODE, bool FIELD, bool BGK> __host__ __device__ constexpr bool tile_two_items() {
-    return sizeof(S) == 2 && MODE == 0 && !FIELD && !BGK;
-}
-
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
 __global__ void __launch_bounds__(256, tile_min_blocks<S, MODE, FIELD, BGK>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if constexpr (tile_two_items<S, MODE, FIELD, BGK>()) tile_item2<LT, S, FORCE>(a, 2u * w, threadIdx.x & 31u);
-    else tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, w, threadIdx.x & 31u);
+    tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
 }
 
 

@@ -38,8 +38,8 @@ struct StageArgs {
     uint32_t nblocks;     // blocks of up to R interior rows
     uint32_t rows;        // R
     uint32_t yblocks;     // blocks per z plane
-    FastDiv div_yblocks, div_nxi; // div_nxi: work units per row in the main loop (node pairs with 16/32-bit
-                                  // storage; else nodes: nx, or nx - 2 with x walls)
+    FastDiv div_yblocks, div_nxi; // div_nxi: work units per row in the main loop (nx / 2 node pairs with
+                                  // 16/32-bit storage; else nodes: nx, or nx - 2 with x walls)
     uint32_t stages;      // S (2 .. STAGE_MAX)
     uint32_t stage_elems; // Q R nx
     double om1;
@@ -108,12 +108,61 @@ constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
 // stage (empty barrier, one arrive per warp), then issues the block's bulk
 // copies onto the stage's full barrier.  The compute warps wait on the full
 // barrier, compute, and release the stage; no barrier over the whole CTA.
-// resident CTAs per SM: the packed-pair compute of 16/32-bit storage keeps
-// two nodes live per thread (2 CTAs, up to 113 registers); FP64 at 3
-template <typename S> constexpr int stage_min_blocks() { return sizeof(S) <= 4 ? 2 : 3; }
+// registers per thread: the packed-pair compute of 16/32-bit storage keeps
+// two nodes live per thread (112: 2 CTAs of 288 threads per SM); FP64 72 (3)
+template <typename S> __host__ __device__ constexpr int stage_max_regs() { return sizeof(S) <= 4 ? 112 : 72; }
+
+// the two x ends of row r as one pair: the x = nx-1 node in the low lane,
+// the x = 0 node in the high lane (periodic x: the upstream values wrap
+// inside the row; x walls: the entering populations bounce back from the
+// gathered sources, then each face's closure)
+template <class LT, typename S, bool FORCE>
+__device__ __noinline__ void stage_end_pair(const StageArgs<LT::Q, S> &a, const S *st, const S *wb, int z, int y0,
+                                            int r) {
+    const Geom &g = a.g;
+    const int nx = g.nx;
+    const uint32_t R = a.rows;
+    const bool xwall = g.face[0] != FACE_PERIODIC;
+    const S *row = st + (size_t)r * nx;
+    const uint32_t row0 = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx;
+    F2 d[LT::Q];
+    if (!xwall) {
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int cx = LT::cx(i);
+            const int xa = cx < 0 ? 0 : nx - 1 - cx, xb = cx > 0 ? nx - 1 : -cx;
+            d[i] = F2(ld_dev<float>(row + (size_t)i * R * nx + xa), ld_dev<float>(row + (size_t)i * R * nx + xb));
+        });
+    } else {
+        constexpr uint32_t M0 = entering_mask<LT, 0>(), M1 = entering_mask<LT, 1>();
+        const float u0x = float(g.uw[0][0]), u0y = float(g.uw[0][1]), u0z = float(g.uw[0][2]);
+        const float u1x = float(g.uw[1][0]), u1y = float(g.uw[1][1]), u1z = float(g.uw[1][2]);
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int cx = LT::cx(i), cy = LT::cy(i), cz = LT::cz(i);
+            float lo, hi;
+            if constexpr (((M1 >> i) & 1u) != 0) {
+                const float v = ld_dev<float>(wb + ((size_t)1 * LT::Q + i) * R + r);
+                lo = v + float(6) * (float(cx) * u1x + float(cy) * u1y + float(cz) * u1z);
+            } else {
+                lo = ld_dev<float>(row + (size_t)i * R * nx + (nx - 1 - cx));
+            }
+            if constexpr (((M0 >> i) & 1u) != 0) {
+                const float v = ld_dev<float>(wb + (size_t)i * R + r);
+                hi = v + float(6) * (float(cx) * u0x + float(cy) * u0y + float(cz) * u0z);
+            } else {
+                hi = ld_dev<float>(row + (size_t)i * R * nx + (0 - cx));
+            }
+            d[i] = F2(lo, hi);
+        });
+        const uint32_t mlo = g.face[1] == FACE_WALL ? M1 : 0u, mhi = g.face[0] == FACE_WALL ? M0 : 0u;
+        if (mlo | mhi) regularize_pair<LT, FORCE, M0 | M1>(d, mlo, mhi, F2(a.F[0]), F2(a.F[1]), F2(a.F[2]));
+    }
+    pair_core<LT, S, FORCE>(d, row0 + (uint32_t)nx - 1u, row0, a.dst, a.om1, a.F, a.status, g.sround != 0);
+}
 
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(STAGE_THREADS, stage_min_blocks<S>())
+__global__ void __maxnreg__(stage_max_regs<S>())
     stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
@@ -202,9 +251,9 @@ __global__ void __launch_bounds__(STAGE_THREADS, stage_min_blocks<S>())
         return;
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
-    // 16- and 32-bit storage: the x in [1, nx-2] of a row as packed pairs
-    // (1 + 2p, 2 + 2p) read from the stage (a population's row starts at an
-    // even element: nx is even), x = 0 and x = nx-1 one node per thread
+    // 16- and 32-bit storage: a row as nx / 2 packed pairs, (1 + 2p, 2 + 2p)
+    // read from the stage (a population's row starts at an even element: nx
+    // is even) and the end pair (nx-1, 0)
     constexpr bool PAIR = sizeof(S) <= 4;
     // one node (r, x) of the block: the stage's row r, a periodic x wrapping
     // inside the row, an x wall through the gathered bounce-back sources
@@ -273,18 +322,23 @@ __global__ void __launch_bounds__(STAGE_THREADS, stage_min_blocks<S>())
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
         const S *wb = wall + (size_t)(k % NS) * wall_elems;
-        // the main loop: node pairs (or nodes) of the block's rows; the x = 0
-        // and x = nx-1 nodes of the pair layout, or the x-wall nodes, go to
-        // two warps of their own (x = 0, x = nx - 1) after it
-        const int nxi = PAIR ? (nx - 2) / 2 : (xwall ? nx - 2 : nx);
+        // the main loop: per row the node pairs (1 + 2p, 2 + 2p) and the end
+        // pair (nx-1, 0) with 16/32-bit storage; else the nodes, the x-wall
+        // nodes going to two warps of their own (x = 0, x = nx - 1) after it
+        const int nxi = PAIR ? nx / 2 : (xwall ? nx - 2 : nx);
         const int nmain = rows * nxi;
-        const int nends = (PAIR || xwall) ? 2 * 32 : 0;
+        const int nends = (!PAIR && xwall) ? 2 * 32 : 0;
         const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nends;
         for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
             if (t < nmain) {
                 const int r = (int)fdiv((uint32_t)t, a.div_nxi);
                 if constexpr (PAIR) {
-                    const int x = 1 + 2 * (t - r * nxi);
+                    const int p = t - r * nxi;
+                    if (p == nxi - 1) {
+                        stage_end_pair<LT, S, FORCE>(a, st, wb, z, y0, r);
+                        continue;
+                    }
+                    const int x = 1 + 2 * p;
                     const S *row = st + (size_t)r * nx;
                     F2 d[LT::Q];
                     static_for<LT::Q>([&](auto ic) {
@@ -293,11 +347,11 @@ __global__ void __launch_bounds__(STAGE_THREADS, stage_min_blocks<S>())
                     });
                     const uint32_t idx =
                         ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx + (uint32_t)x;
-                    pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, g.sround != 0);
+                    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, g.sround != 0);
                 } else {
                     node(st, wb, z, y0, r, (xwall ? 1 : 0) + t - r * nxi);
                 }
-            } else {
+            } else if constexpr (!PAIR) {
                 const int w = t - (total - nends);
                 if (w < 0) continue; // padding of the main loop's last round
                 const int r = w & 31;
