@@ -620,56 +620,6 @@ __device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, uint32_t 
     store_pair<LT, S>(dst, ia, ib, d, sround, sr_seed(ia, m.drho.lo(), ux.lo()), sr_seed(ib, m.drho.hi(), ux.hi()));
 }
 
-// the populations of the pair x, x + 1 (x odd) streamed in from row, a run
-// of the source values of one population starting at an even element
-template <class LT, typename S, int I>
-__device__ __forceinline__ F2 pull_pair(const S *row, int x) {
-    if constexpr (LT::cx(I) == 0) return F2(ld_dev<float>(row + x), ld_dev<float>(row + x + 1));
-    else return ld_pair<S>(row + (x - LT::cx(I)));
-}
-
-// The regularized closure (regularize) of a node pair whose two nodes lie on
-// different wall faces: the closure value of every population in CMASK is
-// formed for both lanes, and each lane takes it where its own mask (mlo, mhi)
-// has the population.  Lane by lane this is regularize() of that node.
-template <class LT, bool FORCE, uint32_t CMASK>
-__device__ __forceinline__ void regularize_pair(F2 (&d)[LT::Q], uint32_t mlo, uint32_t mhi, F2 Fx, F2 Fy, F2 Fz) {
-    using T = F2;
-    Mom<T> m = moments<LT>(d);
-    T ux, uy, uz;
-    velocity(m, Fx, Fy, Fz, ux, uy, uz);
-    const T rho = T(1) + m.drho;
-    T n[6];
-    aneq_base(m, rho, ux, uy, uz, n);
-    T Aq[6], Bq[10];
-    eq_coeffs(rho, ux, uy, uz, Aq, Bq);
-    T Fe = T(0);
-    if constexpr (FORCE) {
-        Fe = T(-1.5) * (ux * Fx + uy * Fy + uz * Fz);
-        T C[6];
-        force_correction<LT>(m.drho, Aq, Bq, Fe, Fx, Fy, Fz, C);
-#pragma unroll
-        for (int k = 0; k < 6; k++) n[k] += C[k];
-    }
-    T Bn[10];
-    third_from_second(n, ux, uy, uz, T(1), Bn);
-    const uint32_t mask = mlo | mhi;
-    static_for<LT::Q>([&](auto ic) {
-        constexpr int i = decltype(ic)::value;
-        if constexpr (((CMASK >> i) & 1u) != 0)
-        if ((mask >> i) & 1u) {
-            T Ee = m.drho + even_poly<LT, i>(Aq);
-            T Eo = odd_poly<LT, i>(Bq);
-            T v = Ee + Eo + even_poly<LT, i>(n) + odd_poly<LT, i, T, false>(Bn);
-            if constexpr (FORCE) {
-                T Fo = T(1.5) * (T(LT::cx(i)) * Fx + T(LT::cy(i)) * Fy + T(LT::cz(i)) * Fz);
-                v -= (T(1) + Ee + Eo) * (Fe + Fo);
-            }
-            d[i] = F2(((mlo >> i) & 1u) ? v.lo() : d[i].lo(), ((mhi >> i) & 1u) ? v.hi() : d[i].hi());
-        }
-    });
-}
-
 template <class LT, typename S, bool FORCE, class A>
 __device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
     F2 d[LT::Q];

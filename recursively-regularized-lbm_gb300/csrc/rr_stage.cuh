@@ -38,8 +38,7 @@ struct StageArgs {
     uint32_t nblocks;     // blocks of up to R interior rows
     uint32_t rows;        // R
     uint32_t yblocks;     // blocks per z plane
-    FastDiv div_yblocks, div_nxi; // div_nxi: work units per row in the main loop (nx / 2 node pairs with
-                                  // 16/32-bit storage; else nodes: nx, or nx - 2 with x walls)
+    FastDiv div_yblocks, div_nxi; // div_nxi: nodes per row in the main loop (nx, or nx - 2 with x walls)
     uint32_t stages;      // S (2 .. STAGE_MAX)
     uint32_t stage_elems; // Q R nx
     double om1;
@@ -108,62 +107,8 @@ constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
 // stage (empty barrier, one arrive per warp), then issues the block's bulk
 // copies onto the stage's full barrier.  The compute warps wait on the full
 // barrier, compute, and release the stage; no barrier over the whole CTA.
-// registers per thread: the packed-pair compute of 16/32-bit storage keeps
-// two nodes live per thread (112: 2 CTAs of 288 threads per SM); FP64 72 (3)
-template <typename S> __host__ __device__ constexpr int stage_max_regs() { return sizeof(S) <= 4 ? 112 : 72; }
-
-// the two x ends of row r as one pair: the x = nx-1 node in the low lane,
-// the x = 0 node in the high lane (periodic x: the upstream values wrap
-// inside the row; x walls: the entering populations bounce back from the
-// gathered sources, then each face's closure)
 template <class LT, typename S, bool FORCE>
-__device__ __noinline__ void stage_end_pair(const StageArgs<LT::Q, S> &a, const S *st, const S *wb, int z, int y0,
-                                            int r) {
-    const Geom &g = a.g;
-    const int nx = g.nx;
-    const uint32_t R = a.rows;
-    const bool xwall = g.face[0] != FACE_PERIODIC;
-    const S *row = st + (size_t)r * nx;
-    const uint32_t row0 = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx;
-    F2 d[LT::Q];
-    if (!xwall) {
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            constexpr int cx = LT::cx(i);
-            const int xa = cx < 0 ? 0 : nx - 1 - cx, xb = cx > 0 ? nx - 1 : -cx;
-            d[i] = F2(ld_dev<float>(row + (size_t)i * R * nx + xa), ld_dev<float>(row + (size_t)i * R * nx + xb));
-        });
-    } else {
-        constexpr uint32_t M0 = entering_mask<LT, 0>(), M1 = entering_mask<LT, 1>();
-        const float u0x = float(g.uw[0][0]), u0y = float(g.uw[0][1]), u0z = float(g.uw[0][2]);
-        const float u1x = float(g.uw[1][0]), u1y = float(g.uw[1][1]), u1z = float(g.uw[1][2]);
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            constexpr int cx = LT::cx(i), cy = LT::cy(i), cz = LT::cz(i);
-            float lo, hi;
-            if constexpr (((M1 >> i) & 1u) != 0) {
-                const float v = ld_dev<float>(wb + ((size_t)1 * LT::Q + i) * R + r);
-                lo = v + float(6) * (float(cx) * u1x + float(cy) * u1y + float(cz) * u1z);
-            } else {
-                lo = ld_dev<float>(row + (size_t)i * R * nx + (nx - 1 - cx));
-            }
-            if constexpr (((M0 >> i) & 1u) != 0) {
-                const float v = ld_dev<float>(wb + (size_t)i * R + r);
-                hi = v + float(6) * (float(cx) * u0x + float(cy) * u0y + float(cz) * u0z);
-            } else {
-                hi = ld_dev<float>(row + (size_t)i * R * nx + (0 - cx));
-            }
-            d[i] = F2(lo, hi);
-        });
-        const uint32_t mlo = g.face[1] == FACE_WALL ? M1 : 0u, mhi = g.face[0] == FACE_WALL ? M0 : 0u;
-        if (mlo | mhi) regularize_pair<LT, FORCE, M0 | M1>(d, mlo, mhi, F2(a.F[0]), F2(a.F[1]), F2(a.F[2]));
-    }
-    pair_core<LT, S, FORCE>(d, row0 + (uint32_t)nx - 1u, row0, a.dst, a.om1, a.F, a.status, g.sround != 0);
-}
-
-template <class LT, typename S, bool FORCE>
-__global__ void __maxnreg__(stage_max_regs<S>())
-    stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(stage_smem);  // [STAGE_MAX]
@@ -251,68 +196,6 @@ __global__ void __maxnreg__(stage_max_regs<S>())
         return;
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
-    // 16- and 32-bit storage: a row as nx / 2 packed pairs, (1 + 2p, 2 + 2p)
-    // read from the stage (a population's row starts at an even element: nx
-    // is even) and the end pair (nx-1, 0)
-    constexpr bool PAIR = sizeof(S) <= 4;
-    // one node (r, x) of the block: the stage's row r, a periodic x wrapping
-    // inside the row, an x wall through the gathered bounce-back sources
-    auto node = [&](const S *st, const S *wb, int z, int y0, int r, int x) {
-        const int y = y0 + r;
-        const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
-        const S *row = st + (size_t)r * nx;
-        T d[LT::Q];
-        if (x >= 1 && x <= nx - 2) {
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
-            });
-        } else if (!xwall) {
-            // periodic x: the upstream node of an x-face node wraps inside the row
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                int xs = x - LT::cx(i);
-                xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
-                d[i] = ld_dev<T>(row + (size_t)i * R * nx + xs);
-            });
-        } else {
-            // an x wall: the entering populations bounce back from this
-            // node's own post-collision values (gathered into the stage by
-            // the producer), then the face's closure
-            auto wallnode = [&](auto fc) {
-                constexpr int F = decltype(fc)::value;
-                constexpr uint32_t M = entering_mask<LT, F>();
-                const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
-                static_for<LT::Q>([&](auto ic) {
-                    constexpr int i = decltype(ic)::value;
-                    if constexpr (((M >> i) & 1u) != 0) {
-                        const T v = ld_dev<T>(wb + ((size_t)F * LT::Q + i) * R + r);
-                        d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
-                    } else {
-                        d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
-                    }
-                });
-                if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
-            };
-            if (x == 0) wallnode(std::integral_constant<int, 0>{});
-            else wallnode(std::integral_constant<int, 1>{});
-        }
-        Mom<T> m = moments<LT>(d);
-        T ux, uy, uz;
-        velocity(m, Fx, Fy, Fz, ux, uy, uz);
-        if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
-        collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
-        if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
-            if (g.sround) {
-                store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
-                return;
-            }
-        }
-        static_for<LT::Q>([&](auto ic) {
-            constexpr int i = decltype(ic)::value;
-            st_dev<T>(a.dst[i] + idx, d[i]);
-        });
-    };
     for (uint32_t k = 0; k < mine; k++) {
         if (!mbar_wait(&full[k % NS], (k / NS) & 1u, a.wait_limit)) {
             if ((threadIdx.x & 31u) == 0) atomicOr(a.status, WATCH_STAGE_WAIT);
@@ -322,42 +205,78 @@ __global__ void __maxnreg__(stage_max_regs<S>())
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
         const S *wb = wall + (size_t)(k % NS) * wall_elems;
-        // the main loop: per row the node pairs (1 + 2p, 2 + 2p) and the end
-        // pair (nx-1, 0) with 16/32-bit storage; else the nodes, the x-wall
-        // nodes going to two warps of their own (x = 0, x = nx - 1) after it
-        const int nxi = PAIR ? nx / 2 : (xwall ? nx - 2 : nx);
+        // the main loop takes every node of the block's rows, or with x walls
+        // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
+        const int nxi = xwall ? nx - 2 : nx;
         const int nmain = rows * nxi;
-        const int nends = (!PAIR && xwall) ? 2 * 32 : 0;
-        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nends;
+        const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
+        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nwall;
         for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
+            int r, x;
             if (t < nmain) {
-                const int r = (int)fdiv((uint32_t)t, a.div_nxi);
-                if constexpr (PAIR) {
-                    const int p = t - r * nxi;
-                    if (p == nxi - 1) {
-                        stage_end_pair<LT, S, FORCE>(a, st, wb, z, y0, r);
-                        continue;
-                    }
-                    const int x = 1 + 2 * p;
-                    const S *row = st + (size_t)r * nx;
-                    F2 d[LT::Q];
+                r = (int)fdiv((uint32_t)t, a.div_nxi);
+                x = (xwall ? 1 : 0) + t - r * nxi;
+            } else {
+                const int w = t - (total - nwall);
+                if (w < 0) continue;        // padding of the main loop's last round
+                r = w & 31;
+                if (r >= rows) continue;
+                x = w < 32 ? 0 : nx - 1;
+            }
+            const int y = y0 + r;
+            const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
+            const S *row = st + (size_t)r * nx;
+            T d[LT::Q];
+            if (x >= 1 && x <= nx - 2) {
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+                });
+            } else if (!xwall) {
+                // periodic x: the upstream node of an x-face node wraps inside the row
+                static_for<LT::Q>([&](auto ic) {
+                    constexpr int i = decltype(ic)::value;
+                    int xs = x - LT::cx(i);
+                    xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
+                    d[i] = ld_dev<T>(row + (size_t)i * R * nx + xs);
+                });
+            } else {
+                // an x wall: the entering populations bounce back from this
+                // node's own post-collision values (gathered into the stage by
+                // the producer), then the face's closure
+                auto wallnode = [&](auto fc) {
+                    constexpr int F = decltype(fc)::value;
+                    constexpr uint32_t M = entering_mask<LT, F>();
+                    const T ux = T(g.uw[F][0]), uy = T(g.uw[F][1]), uz = T(g.uw[F][2]);
                     static_for<LT::Q>([&](auto ic) {
                         constexpr int i = decltype(ic)::value;
-                        d[i] = pull_pair<LT, S, i>(row + (size_t)i * R * nx, x);
+                        if constexpr (((M >> i) & 1u) != 0) {
+                            const T v = ld_dev<T>(wb + ((size_t)F * LT::Q + i) * R + r);
+                            d[i] = v + T(6) * (T(LT::cx(i)) * ux + T(LT::cy(i)) * uy + T(LT::cz(i)) * uz);
+                        } else {
+                            d[i] = ld_dev<T>(row + (size_t)i * R * nx + (x - LT::cx(i)));
+                        }
                     });
-                    const uint32_t idx =
-                        ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx + (uint32_t)x;
-                    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, g.sround != 0);
-                } else {
-                    node(st, wb, z, y0, r, (xwall ? 1 : 0) + t - r * nxi);
-                }
-            } else if constexpr (!PAIR) {
-                const int w = t - (total - nends);
-                if (w < 0) continue; // padding of the main loop's last round
-                const int r = w & 31;
-                if (r >= rows) continue;
-                node(st, wb, z, y0, r, w < 32 ? 0 : nx - 1);
+                    if (g.face[F] == FACE_WALL) regularize<LT, T, FORCE, M>(d, M, Fx, Fy, Fz);
+                };
+                if (x == 0) wallnode(std::integral_constant<int, 0>{});
+                else wallnode(std::integral_constant<int, 1>{});
             }
+            Mom<T> m = moments<LT>(d);
+            T ux, uy, uz;
+            velocity(m, Fx, Fy, Fz, ux, uy, uz);
+            if (!(m.drho > T(-0.9) && m.drho < T(9))) atomicOr(a.status, 1);
+            collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
+            if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
+                if (g.sround) {
+                    store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
+                    continue;
+                }
+            }
+            static_for<LT::Q>([&](auto ic) {
+                constexpr int i = decltype(ic)::value;
+                st_dev<T>(a.dst[i] + idx, d[i]);
+            });
         }
         // this warp is done with stage k % NS
         __syncwarp();

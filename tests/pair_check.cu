@@ -1,8 +1,8 @@
 // pair_check.cu -- the packed FP32-pair node arithmetic (csrc/rr_pair.cuh)
 // against the scalar FP32 node arithmetic on the GPU, bit for bit: moments,
 // velocity, the second- and third-order coefficients, the full collision
-// (force-free and forced, D3Q27), the wall closure of a pair on two faces and
-// the stochastically rounded 16-bit stores, for 65,536 random node pairs.  Built with
+// (force-free and forced, D3Q27) and the stochastically rounded 16-bit stores,
+// for 65,536 random node pairs.  Built with
 // the library's flags and run by tests/test_gpu_pair.py; prints the mismatch
 // bits (0: none) and exits 1 on a mismatch.
 #include <cstdio>
@@ -54,25 +54,6 @@ __global__ void check(int *bad, int n) {
     eq_coeffs(F2(1.0f) + m2.drho, ux2, uy2, uz2, Aq2, Bq2);
     for (int k = 0; k < 6; k++) if (__float_as_uint(Aq[k]) != __float_as_uint(Aq2[k].lo())) atomicOr(bad, 16);
     for (int k = 0; k < 10; k++) if (__float_as_uint(Bq[k]) != __float_as_uint(Bq2[k].lo())) atomicOr(bad, 32);
-    // the wall closure of two nodes on the x-hi (low lane) and x-lo (high
-    // lane) faces, as the staged step's end pair computes it
-    {
-        constexpr uint32_t M0 = entering_mask<L27, 0>(), M1 = entering_mask<L27, 1>();
-        float ra[27], rb[27];
-        F2 r2[27];
-        for (int i = 0; i < 27; i++) {
-            ra[i] = 0.02f * rnd(t * 64 + 7 + i);
-            rb[i] = 0.02f * rnd(t * 64 + 39 + i);
-            r2[i] = F2(ra[i], rb[i]);
-        }
-        regularize<L27, float, FORCE, M1>(ra, M1, Fx, Fy, Fz);
-        regularize<L27, float, FORCE, M0>(rb, M0, Fx, Fy, Fz);
-        regularize_pair<L27, FORCE, M0 | M1>(r2, M1, M0, F2(Fx), F2(Fy), F2(Fz));
-        for (int i = 0; i < 27; i++)
-            if (__float_as_uint(ra[i]) != __float_as_uint(r2[i].lo()) ||
-                __float_as_uint(rb[i]) != __float_as_uint(r2[i].hi()))
-                atomicOr(bad, 256);
-    }
     float Bn[10]; F2 Bn2[10];
     third_from_second(nn, uxa, uya, uza, om1, Bn);
     third_from_second(n2, ux2, uy2, uz2, F2(om1), Bn2);
@@ -129,6 +110,6 @@ int main() {
     cudaFree(ha);
     cudaFree(ba);
     printf("pair vs scalar mismatch bits: force-free / FP16 stores %d, forced / BF16 stores %d "
-           "(1 moments, 2 velocity, 4 collision, 8 aneq, 16 Aq, 32 Bq, 64 Bn, 128 rounded stores, 256 wall closure)\n", h[0], h[1]);
+           "(1 moments, 2 velocity, 4 collision, 8 aneq, 16 Aq, 32 Bq, 64 Bn, 128 rounded stores)\n", h[0], h[1]);
     return (h[0] || h[1]) ? 1 : 0;
 }
