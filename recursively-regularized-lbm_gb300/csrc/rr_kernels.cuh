@@ -365,19 +365,19 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 }
 
 // resident CTAs per SM the tile step is compiled for (register budget 65536 /
-// (256 x that)).  The DNS step and the WALE passes of 16- and 32-bit storage
-// carry the packed pair path (two nodes' populations live per thread): 2
-// CTAs, 128 registers.  The BGK step runs one node per thread at 5, the
-// trip-forcing steps (per-node force fields) at 4 (DNS) and 5 (WALE).
-#ifndef RR_PAIR_MIN_BLOCKS
-#define RR_PAIR_MIN_BLOCKS 2
-#endif
+// (256 x that)).  The DNS step of 16- and 32-bit storage carries the packed
+// pair path (two nodes' populations live per thread): FP16/BF16 at 3 CTAs,
+// 80 registers (at 2 CTAs, 128 registers, 2 % slower), FP32 at 2 (its pairs
+// of FP32 loads take twice the registers).  The WALE passes and the BGK step
+// run one node per thread at 5, the trip-forcing step (per-node force
+// fields) at 4.
+template <typename S> __host__ __device__ constexpr int pair_min_blocks() { return sizeof(S) == 2 ? 3 : 2; }
 template <typename S, int MODE = 0, bool FIELD = false, bool BGK = false> constexpr int tile_min_blocks() {
-    return sizeof(S) == 8 ? 2 : (FIELD ? (MODE == 0 ? 4 : 5) : BGK ? 5 : RR_PAIR_MIN_BLOCKS);
+    return sizeof(S) == 8 ? 2 : (MODE != 0 ? 5 : FIELD ? 4 : BGK ? 5 : pair_min_blocks<S>());
 }
 // the batch kernel holds its loop state and the shared descriptor on top of
 // the tile step's registers
-template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : RR_PAIR_MIN_BLOCKS; }
+template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : pair_min_blocks<S>(); }
 
 template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
 template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
@@ -604,9 +604,7 @@ __device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, uint32_t 
 // FP32 pairs.  A population with c_x != 0 streams in from x - c_x, an even
 // element offset for both nodes together: one 32-bit (16-bit storage) or
 // 64-bit (FP32) load; the c_x = 0 populations take two scalar loads.  The
-// arithmetic is the scalar node's, lane by lane.  MODE as tile_item: 0 the
-// DNS step; 1 the WALE velocity pass (moments, u to a.u); 2 the WALE collide
-// pass (tau_t of each node from a.u, then the collision).
+// arithmetic is the scalar node's, lane by lane.
 // the DNS step of the node pair ia (low lane), ib (high lane) from its
 // post-stream populations d: moments, the watchdog, the collision, the stores
 template <class LT, typename S, bool FORCE>
@@ -622,9 +620,8 @@ __device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, uint32_t 
     store_pair<LT, S>(dst, ia, ib, d, sround, sr_seed(ia, m.drho.lo(), ux.lo()), sr_seed(ib, m.drho.hi(), ux.hi()));
 }
 
-template <class LT, typename S, bool FORCE, int MODE, class A>
-__device__ __forceinline__ void pair_node(const A &a, uint32_t idx, int x, int y, int z) {
-    const Geom &g = a.g;
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
     F2 d[LT::Q];
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
@@ -632,33 +629,7 @@ __device__ __forceinline__ void pair_node(const A &a, uint32_t idx, int x, int y
         if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
         else d[i] = ld_pair<S>(p);
     });
-    const F2 Fx(a.F[0]), Fy(a.F[1]), Fz(a.F[2]);
-    Mom<F2> m = moments<LT>(d);
-    F2 ux, uy, uz;
-    velocity(m, Fx, Fy, Fz, ux, uy, uz);
-    if constexpr (MODE == 1) {
-        float *u = a.u;
-        u[idx] = ux.lo();
-        u[idx + 1] = ux.hi();
-        u[g.stride + idx] = uy.lo();
-        u[g.stride + idx + 1] = uy.hi();
-        u[2ull * g.stride + idx] = uz.lo();
-        u[2ull * g.stride + idx + 1] = uz.hi();
-        return;
-    }
-    if (!(m.drho.lo() > -0.9f && m.drho.lo() < 9.0f && m.drho.hi() > -0.9f && m.drho.hi() < 9.0f))
-        atomicOr(a.status, 1);
-    F2 om1(a.om1);
-    if constexpr (MODE == 2) {
-        // each node's tau_t and relaxation factor, as the node alone forms them
-        const float cw = float(a.cw), tau = float(a.tau);
-        const float oa = 1.0f - 1.0f / (tau + les_taut<float>(a.u, g, x, y, z, idx, cw));
-        const float ob = 1.0f - 1.0f / (tau + les_taut<float>(a.u, g, x + 1, y, z, idx + 1u, cw));
-        om1 = F2(oa, ob);
-    }
-    collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, om1, Fx, Fy, Fz);
-    store_pair<LT, S>(a.dst, idx, idx + 1u, d, g.sround != 0, sr_seed(idx, m.drho.lo(), ux.lo()),
-                      sr_seed(idx + 1u, m.drho.hi(), ux.hi()));
+    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
 }
 
 // The node(s) a lane of work item `item` takes: false if none.  The slow
@@ -729,17 +700,17 @@ __device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t 
 // takes tau_t from the 7-point stencil of that field and collides.
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
-    // the packed-pair form: 16- and 32-bit storage, the DNS step and the
-    // WALE passes with a uniform force and the RR collision (the host sets
-    // a.pairs only then, and only for an even nx)
-    constexpr bool PAIRABLE = sizeof(S) <= 4 && !FIELD && !BGK;
+    // the packed-pair form: 16- and 32-bit storage, the DNS step with a
+    // uniform force and the RR collision (the host sets a.pairs only then,
+    // and only for an even nx)
+    constexpr bool PAIRABLE = sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
     uint32_t row;
     int x, y, z;
     bool fast, pair;
     if (!tile_decode<PAIRABLE>(a, item, lane, row, x, y, z, fast, pair)) return;
     if constexpr (PAIRABLE) {
         if (pair && fast) {
-            pair_node<LT, S, FORCE, MODE>(a, row * (uint32_t)a.g.nx + (uint32_t)x, x, y, z);
+            pair_node<LT, S, FORCE>(a, row * (uint32_t)a.g.nx + (uint32_t)x);
             return;
         }
     }

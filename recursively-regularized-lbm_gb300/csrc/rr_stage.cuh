@@ -38,8 +38,7 @@ struct StageArgs {
     uint32_t nblocks;     // blocks of up to R interior rows
     uint32_t rows;        // R
     uint32_t yblocks;     // blocks per z plane
-    FastDiv div_yblocks, div_nxi; // div_nxi: work units per row in the main loop ((nx - 2) / 2 node pairs
-                                  // with 16/32-bit storage; else nodes: nx, or nx - 2 with x walls)
+    FastDiv div_yblocks, div_nxi; // div_nxi: nodes per row in the main loop (nx, or nx - 2 with x walls)
     uint32_t stages;      // S (2 .. STAGE_MAX)
     uint32_t stage_elems; // Q R nx
     double om1;
@@ -100,40 +99,16 @@ __device__ __forceinline__ void stage_block(uint32_t b, const FastDiv &div_ybloc
     rows = min((int)R, ny - 1 - y0);
 }
 
-constexpr int STAGE_CONSUMERS = 256; // threads of the main loop (8 compute warps)
+constexpr int STAGE_CONSUMERS = 256;                  // compute threads (8 warps)
+constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
 
-// 16- and 32-bit storage: the main loop takes the x in [1, nx-2] of a row as
-// packed pairs (1 + 2p, 2 + 2p) read from the stage (a population's row
-// starts at an even element: the staged step's rows are a multiple of 16
-// bytes), and a ninth compute warp takes the x = 0 and x = nx-1 nodes of the
-// block's rows, so that the pair warps never diverge into the end nodes' path
-template <typename S> __host__ __device__ constexpr bool stage_pairs() { return sizeof(S) <= 4; }
-template <typename S> __host__ __device__ constexpr int stage_compute_warps() { return stage_pairs<S>() ? 9 : 8; }
-// the compute warps and the producer warp
-template <typename S> __host__ __device__ constexpr int stage_threads() { return 32 * stage_compute_warps<S>() + 32; }
-// resident CTAs per SM: the pair warps keep two nodes live per thread (2 CTAs
-// of 320 threads, up to 102 registers); one node per thread at 3
-template <typename S> __host__ __device__ constexpr int stage_min_blocks() { return stage_pairs<S>() ? 2 : 3; }
-
-// the populations of the pair x, x + 1 (x odd) streamed in from row, a run
-// of the source values of one population starting at an even element
-template <class LT, typename S, int I>
-__device__ __forceinline__ F2 pull_pair(const S *row, int x) {
-    if constexpr (LT::cx(I) == 0) return F2(ld_dev<float>(row + x), ld_dev<float>(row + x + 1));
-    else return ld_pair<S>(row + (x - LT::cx(I)));
-}
-
-// Warp-specialised pipeline.  The warp after the compute warps (its lane 0)
-// is the producer: for each of the CTA's blocks it waits until the compute
-// warps have released the stage (empty barrier, one arrive per warp), then
-// issues the block's bulk copies onto the stage's full barrier.  The compute
-// warps wait on the full barrier, compute, and release the stage; no barrier
-// over the whole CTA.
+// Warp-specialised pipeline.  Warp 8 (its lane 0) is the producer: for each
+// of the CTA's blocks it waits until the 8 compute warps have released the
+// stage (empty barrier, one arrive per warp), then issues the block's bulk
+// copies onto the stage's full barrier.  The compute warps wait on the full
+// barrier, compute, and release the stage; no barrier over the whole CTA.
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(stage_threads<S>(), stage_min_blocks<S>())
-    stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
-    constexpr bool PAIR = stage_pairs<S>();
-    constexpr int CONS = 32 * stage_compute_warps<S>(); // compute threads
+__global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(stage_smem);  // [STAGE_MAX]
@@ -153,14 +128,14 @@ __global__ void __launch_bounds__(stage_threads<S>(), stage_min_blocks<S>())
         for (uint32_t s = 0; s < NS; s++) {
             // the copies' expect_tx arrive, plus the gather's arrive with x walls
             mbar_init(&full[s], xwall ? 2 : 1);
-            mbar_init(&empty[s], CONS / 32);
+            mbar_init(&empty[s], STAGE_CONSUMERS / 32);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     // blocks of this CTA: blockIdx.x + k gridDim.x, k = 0 .. mine-1
     const uint32_t mine = blockIdx.x < a.nblocks ? (a.nblocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    if (threadIdx.x >= CONS) {
+    if (threadIdx.x >= STAGE_CONSUMERS) {
         // the producer warp: lane 0 waits for the stage and issues the bulk
         // copies; with x walls every lane then gathers the wall values (else
         // lane 0 runs alone)
@@ -230,9 +205,24 @@ __global__ void __launch_bounds__(stage_threads<S>(), stage_min_blocks<S>())
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
         const S *wb = wall + (size_t)(k % NS) * wall_elems;
-        // one node (r, x) of the block: the stage's row r, a periodic x
-        // wrapping inside the row, an x wall through the gathered sources
-        auto node = [&](int r, int x) {
+        // the main loop takes every node of the block's rows, or with x walls
+        // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
+        const int nxi = xwall ? nx - 2 : nx;
+        const int nmain = rows * nxi;
+        const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
+        const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nwall;
+        for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
+            int r, x;
+            if (t < nmain) {
+                r = (int)fdiv((uint32_t)t, a.div_nxi);
+                x = (xwall ? 1 : 0) + t - r * nxi;
+            } else {
+                const int w = t - (total - nwall);
+                if (w < 0) continue;        // padding of the main loop's last round
+                r = w & 31;
+                if (r >= rows) continue;
+                x = w < 32 ? 0 : nx - 1;
+            }
             const int y = y0 + r;
             const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
             const S *row = st + (size_t)r * nx;
@@ -280,55 +270,13 @@ __global__ void __launch_bounds__(stage_threads<S>(), stage_min_blocks<S>())
             if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
                 if (g.sround) {
                     store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
-                    return;
+                    continue;
                 }
             }
             static_for<LT::Q>([&](auto ic) {
                 constexpr int i = decltype(ic)::value;
                 st_dev<T>(a.dst[i] + idx, d[i]);
             });
-        };
-        if constexpr (PAIR) {
-            if (threadIdx.x < STAGE_CONSUMERS) {
-                // the pairs (1 + 2p, 2 + 2p) of the block's rows
-                const int npr = (nx - 2) / 2;
-                for (int t = threadIdx.x; t < rows * npr; t += STAGE_CONSUMERS) {
-                    const int r = (int)fdiv((uint32_t)t, a.div_nxi);
-                    const int x = 1 + 2 * (t - r * npr);
-                    const S *row = st + (size_t)r * nx;
-                    F2 d[LT::Q];
-                    static_for<LT::Q>([&](auto ic) {
-                        constexpr int i = decltype(ic)::value;
-                        d[i] = pull_pair<LT, S, i>(row + (size_t)i * R * nx, x);
-                    });
-                    const uint32_t idx =
-                        ((uint32_t)z * (uint32_t)g.ny + (uint32_t)(y0 + r)) * (uint32_t)nx + (uint32_t)x;
-                    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, g.sround != 0);
-                }
-            } else {
-                // the end warp: x = 0 of every row, then x = nx-1
-                for (int e = threadIdx.x - STAGE_CONSUMERS; e < 2 * rows; e += 32)
-                    node(e < rows ? e : e - rows, e < rows ? 0 : nx - 1);
-            }
-        } else {
-            // every node of the block's rows, or with x walls the x in
-            // [1, nx-2] ones; the x-wall nodes go to two warps of their own
-            const int nxi = xwall ? nx - 2 : nx;
-            const int nmain = rows * nxi;
-            const int nwall = xwall ? 2 * 32 : 0; // warps 0 and 1 of a second round: x = 0, x = nx - 1
-            const int total = ((nmain + STAGE_CONSUMERS - 1) / STAGE_CONSUMERS) * STAGE_CONSUMERS + nwall;
-            for (int t = threadIdx.x; t < total; t += STAGE_CONSUMERS) {
-                if (t < nmain) {
-                    const int r = (int)fdiv((uint32_t)t, a.div_nxi);
-                    node(r, (xwall ? 1 : 0) + t - r * nxi);
-                } else {
-                    const int w = t - (total - nwall);
-                    if (w < 0) continue; // padding of the main loop's last round
-                    const int r = w & 31;
-                    if (r >= rows) continue;
-                    node(r, w < 32 ? 0 : nx - 1);
-                }
-            }
         }
         // this warp is done with stage k % NS
         __syncwarp();
