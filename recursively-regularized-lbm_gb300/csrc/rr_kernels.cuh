@@ -365,15 +365,25 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 }
 
 // resident CTAs per SM the tile step is compiled for (register budget 65536 /
-// (256 x that)).  The DNS step of 16- and 32-bit storage carries the packed
-// pair path (two nodes' populations live per thread): FP16/BF16 at 3 CTAs,
-// 80 registers (at 2 CTAs, 128 registers, 2 % slower), FP32 at 2 (its pairs
-// of FP32 loads take twice the registers).  The WALE passes and the BGK step
-// run one node per thread at 5, the trip-forcing step (per-node force
-// fields) at 4.
+// (256 x that)).  The packed-pair form of the DNS step (PAIRS: two nodes'
+// populations live per thread) runs FP16/BF16 at 3 CTAs, 80 registers (at 2
+// CTAs, 128 registers, 2 % slower), FP32 at 2 (its pairs of FP32 loads take
+// twice the registers).  One node per thread: the force-free DNS step at 5
+// (48 registers), the forced one and the trip-forcing step at 4, the WALE
+// passes and the BGK step at 5.
+#ifndef RR_WALE_MIN_BLOCKS
+#define RR_WALE_MIN_BLOCKS 5
+#endif
 template <typename S> __host__ __device__ constexpr int pair_min_blocks() { return sizeof(S) == 2 ? 3 : 2; }
-template <typename S, int MODE = 0, bool FIELD = false, bool BGK = false> constexpr int tile_min_blocks() {
-    return sizeof(S) == 8 ? 2 : (MODE != 0 ? 5 : FIELD ? 4 : BGK ? 5 : pair_min_blocks<S>());
+template <typename S, bool FORCE = false, int MODE = 0, bool FIELD = false, bool BGK = false, bool PAIRS = false>
+constexpr int tile_min_blocks() {
+    return sizeof(S) == 8 ? 2
+           : PAIRS        ? pair_min_blocks<S>()
+           : MODE != 0    ? RR_WALE_MIN_BLOCKS
+           : FIELD        ? 4
+           : BGK          ? 5
+           : FORCE        ? 4
+                          : 5;
 }
 // the batch kernel holds its loop state and the shared descriptor on top of
 // the tile step's registers
@@ -698,12 +708,13 @@ __device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t 
 // DNS step.  The WALE step is two passes over the same items: MODE 1 streams,
 // applies the walls and writes the velocity field; MODE 2 streams again,
 // takes tau_t from the 7-point stencil of that field and collides.
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, class A>
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, bool PAIRS = true,
+          class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
     // the packed-pair form: 16- and 32-bit storage, the DNS step with a
     // uniform force and the RR collision (the host sets a.pairs only then,
-    // and only for an even nx)
-    constexpr bool PAIRABLE = sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
+    // and only for an even nx); PAIRS = false compiles it out
+    constexpr bool PAIRABLE = PAIRS && sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
     uint32_t row;
     int x, y, z;
     bool fast, pair;
@@ -721,9 +732,13 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     for (int k = 0; k < nn; k++) tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x + k, y, z, fast);
 }
 
-template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false>
-__global__ void __launch_bounds__(256, tile_min_blocks<S, MODE, FIELD, BGK>()) tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
-    tile_item<LT, S, FORCE, MODE, FIELD, BGK>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, threadIdx.x & 31u);
+// PAIRS: the DNS step in the packed-pair layout (a.pairs set); else one node
+// per lane, compiled for more resident CTAs
+template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, bool PAIRS = false>
+__global__ void __launch_bounds__(256, tile_min_blocks<S, FORCE, MODE, FIELD, BGK, PAIRS>())
+    tile_kernel(const __grid_constant__ TileArgs<LT::Q, S> a) {
+    tile_item<LT, S, FORCE, MODE, FIELD, BGK, PAIRS>(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                                                     threadIdx.x & 31u);
 }
 
 

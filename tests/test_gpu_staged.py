@@ -1,7 +1,9 @@
 """The staged DNS step (rr_set_stage RR_DNS_STAGED: face rows in one launch,
 interior rows through a shared-memory pipeline of bulk copies) against the
 tile step: the same populations bit for bit (stated tolerance: zero), and
-against the oracle in FP64."""
+against the oracle in FP64.  On the 64-wide grids the tile step computes its
+interior rows as packed FP32 node pairs and the staged step one node per
+thread, so these cases also hold the two arithmetic forms to the same bits."""
 import numpy as np
 import pytest
 
@@ -22,10 +24,15 @@ def _cases():
         presets.taylor_green(L=20, nz=6, tau=0.55, Ma=0.05, q=19, storage="f32"),
         presets.channel(nx=48, ny=18, nz=10, Re_tau=36, les=False, storage="f16", variant="config", amp=0.2),
         presets.cavity(n=8, Re=50, storage="f16", variant="reference"),  # 8 x 8 x 2: no interior row
+        # rows wide enough for the tile step's packed node pairs (the staged
+        # step computes one node per thread): the two forms agree bit for bit
+        presets.cavity(n=64, Re=400, storage="f16"),
+        presets.cavity(n=64, Re=400, storage="f32"),
+        presets.channel(nx=64, ny=18, nz=10, Re_tau=36, les=False, storage="bf16", variant="config", amp=0.2),
     ]
 
 
-@pytest.mark.parametrize("k", range(8))
+@pytest.mark.parametrize("k", range(11))
 @pytest.mark.parametrize("rows,stages", [(None, None), (1, 2), (3, 4)])
 def test_staged_equals_tile(k, rows, stages):
     p, st = _cases()[k]
