@@ -153,7 +153,7 @@ size_t stat_doubles(const rr_params &p) {
 rr_status ensure_aux(rr_solver *s) {
     if (s->aux) return RR_OK;
     const size_t n = s->g.n;
-    if (cudaMalloc(&s->aux, 5 * n * sizeof(double)) != cudaSuccess) {
+    if (cudaMallocAsync(&s->aux, 5 * n * sizeof(double), s->stream) != cudaSuccess) {
         s->aux = nullptr;
         cudaGetLastError();
         return fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of readout scratch", 5 * n * sizeof(double));
@@ -484,7 +484,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     s->home = s->stream;
     const size_t bytes = (size_t)p->q * g.stride * s->ops->elem_bytes;
     for (int b = 0; b < 2; b++) {
-        if (cudaMalloc(&s->buf[b], bytes) != cudaSuccess) {
+        if (cudaMallocAsync(&s->buf[b], bytes, s->stream) != cudaSuccess) {
             cudaGetLastError();
             s->buf[b] = nullptr;
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of populations", bytes));
@@ -492,16 +492,16 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         s->bytes += bytes;
     }
     // one 256-byte block: the watchdog word, then the 27-entry population order
-    if (cudaMalloc(&s->status, 256) != cudaSuccess || cudaMemset(s->status, 0, 256) != cudaSuccess) {
+    if (cudaMallocAsync(&s->status, 256, s->stream) != cudaSuccess || cudaMemsetAsync(s->status, 0, 256, s->stream) != cudaSuccess) {
         cudaGetLastError();
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the watchdog word"));
     }
     s->pos = s->status + 4;
     std::vector<int> pos = api_positions(*p);
-    if (cudaMemcpy(s->pos, pos.data(), pos.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpyAsync(s->pos, pos.data(), pos.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
         return cleanup(fail(RR_ERR_CUDA, "cannot upload the population order"));
     const size_t sd = stat_doubles(*p) * sizeof(double);
-    if (cudaMalloc(&s->stat, sd) != cudaSuccess || cudaMemset(s->stat, 0, sd) != cudaSuccess) {
+    if (cudaMallocAsync(&s->stat, sd, s->stream) != cudaSuccess || cudaMemsetAsync(s->stat, 0, sd, s->stream) != cudaSuccess) {
         cudaGetLastError();
         return cleanup(fail(RR_ERR_NOMEM, "cannot allocate statistics buffers"));
     }
@@ -523,12 +523,12 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
             }
         if (!edges.empty()) {
             const size_t lb = edges.size() * sizeof(uint32_t);
-            if (cudaMalloc(&s->edge_list, lb) != cudaSuccess) {
+            if (cudaMallocAsync(&s->edge_list, lb, s->stream) != cudaSuccess) {
                 cudaGetLastError();
                 s->edge_list = nullptr;
                 return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the edge-node list"));
             }
-            if (cudaMemcpy(s->edge_list, edges.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+            if (cudaMemcpyAsync(s->edge_list, edges.data(), lb, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
                 return cleanup(fail(RR_ERR_CUDA, "cannot upload the edge-node list"));
             s->nedges = (uint32_t)edges.size();
             s->bytes += lb;
@@ -555,12 +555,12 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
             }
         for (auto &v : by_kind) frows.insert(frows.end(), v.begin(), v.end());
         const size_t lb = frows.size() * sizeof(uint32_t);
-        if (cudaMalloc(&s->frow_list, lb) != cudaSuccess) {
+        if (cudaMallocAsync(&s->frow_list, lb, s->stream) != cudaSuccess) {
             cudaGetLastError();
             s->frow_list = nullptr;
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the face-row list"));
         }
-        if (cudaMemcpy(s->frow_list, frows.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMemcpyAsync(s->frow_list, frows.data(), lb, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
             return cleanup(fail(RR_ERR_CUDA, "cannot upload the face-row list"));
         s->nfrows = (uint32_t)frows.size();
         s->bytes += lb;
@@ -575,12 +575,12 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
         std::vector<uint32_t> all(g.n);
         for (uint32_t i = 0; i < g.n; i++) all[i] = i;
         const size_t lb = all.size() * sizeof(uint32_t);
-        if (cudaMalloc(&s->all_list, lb) != cudaSuccess) {
+        if (cudaMallocAsync(&s->all_list, lb, s->stream) != cudaSuccess) {
             cudaGetLastError();
             s->all_list = nullptr;
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate the node list"));
         }
-        if (cudaMemcpy(s->all_list, all.data(), lb, cudaMemcpyHostToDevice) != cudaSuccess)
+        if (cudaMemcpyAsync(s->all_list, all.data(), lb, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
             return cleanup(fail(RR_ERR_CUDA, "cannot upload the node list"));
         s->all.count = g.n;
         s->all.list = s->all_list;
@@ -589,7 +589,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     g.sround = (p->rounding == RR_ROUND_STOCHASTIC) ? 1 : 0;
     g.bgk = p->collision == RR_COLL_BGK ? 1 : 0;
     if (const size_t ub = les_ubuf_bytes(*p)) {
-        if (cudaMalloc(&s->ubuf, ub) != cudaSuccess) {
+        if (cudaMallocAsync(&s->ubuf, ub, s->stream) != cudaSuccess) {
             cudaGetLastError();
             s->ubuf = nullptr;
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of WALE velocity field", ub));
@@ -605,8 +605,8 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     g.fdbc = s->fdbc;
     if (s->fdbc && p->use_les) {
         const size_t slot = 2 * (size_t)p->lx * p->lz;
-        if (cudaMalloc(&s->fdbc_wt_mem, 2 * slot * sizeof(double)) != cudaSuccess ||
-            cudaMemset(s->fdbc_wt_mem, 0, 2 * slot * sizeof(double)) != cudaSuccess) {
+        if (cudaMallocAsync(&s->fdbc_wt_mem, 2 * slot * sizeof(double), s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->fdbc_wt_mem, 0, 2 * slot * sizeof(double), s->stream) != cudaSuccess) {
             cudaGetLastError();
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of wall tau_t", 2 * slot * sizeof(double)));
         }
@@ -616,7 +616,7 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     }
     if (p->trip_steps > 0) {
         const size_t fb = 6 * (size_t)g.stride * sizeof(double);
-        if (cudaMalloc(&s->ffield, fb) != cudaSuccess) {
+        if (cudaMallocAsync(&s->ffield, fb, s->stream) != cudaSuccess) {
             cudaGetLastError();
             s->ffield = nullptr;
             return cleanup(fail(RR_ERR_NOMEM, "cannot allocate %zu bytes of trip force fields", fb));
@@ -631,6 +631,11 @@ rr_status rr_create(const rr_params *p, rr_solver **out) {
     rr::tuned_les_tile(*p, &s->tile);
     if (s->frow_list) rr::tuned_stage(*p, &s->dns_method, &s->stage_rows, &s->stages);
     rr::tuned_rows_group(*p, &s->rows_group);
+    // the allocations and uploads above are ordered on the solver's stream
+    // (stream-ordered allocation: creating or destroying a solver never waits
+    // for other solvers' work on the device); complete them here
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess)
+        return cleanup(fail(RR_ERR_CUDA, "solver set-up failed: %s", cudaGetErrorString(cudaGetLastError())));
     *out = s;
     return RR_OK;
 }
@@ -641,17 +646,14 @@ rr_status rr_destroy(rr_solver *s) {
     if (s->batch) rr::batch_detach(s);
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
-    cudaFree(s->buf[0]);
-    cudaFree(s->buf[1]);
-    cudaFree(s->status);
-    cudaFree(s->aux);
-    cudaFree(s->stat);
-    cudaFree(s->all_list);
-    cudaFree(s->edge_list);
-    cudaFree(s->ubuf);
-    cudaFree(s->frow_list);
-    cudaFree(s->ffield);
-    cudaFree(s->fdbc_wt_mem);
+    // stream-ordered frees on the solver's own stream: no device-wide wait
+    void *mem[] = {s->buf[0],  s->buf[1],   s->status,    s->aux,    s->stat,       s->all_list,
+                   s->edge_list, s->ubuf, s->frow_list, s->ffield, s->fdbc_wt_mem};
+    for (void *m : mem)
+        if (m) {
+            if (s->home) cudaFreeAsync(m, s->home);
+            else cudaFree(m);
+        }
     if (s->side) {
         cudaStreamSynchronize(s->side);
         cudaStreamDestroy(s->side);

@@ -78,7 +78,10 @@ class GpuBackend:
         from .workloads import macros_on_device, params_of
 
         s = self._rr.Solver(params_of(d))
-        fields = macros_on_device(d, f"cuda:{self.device}")
+        # generated on torch's stream, read by the solver's upload on its own
+        # stream after an event: no host synchronisation with the other
+        # resident domains' work
+        fields = macros_on_device(d, f"cuda:{self.device}", stream=s.stream)
         s.init_state(*fields)
         h = _Member(s, fields)
         self.members.append(h)

@@ -95,14 +95,21 @@ def velocity_scale(d):
     return 1.5 * 15.7 * CHANNEL_USTAR
 
 
-def macros_on_device(d, device="cuda"):
+def macros_on_device(d, device="cuda", stream=None):
     """(rho, ux, uy, uz) FP64 tensors of shape (n, n, n) (z, y, x) on the
-    device, complete when this returns (the solver reads them on its own
-    stream)."""
+    device.  With stream (a cudaStream_t handle, e.g. a solver's) that stream
+    is made to wait for the fields on the device, and nothing blocks the
+    host; without it the fields are complete when this returns.  Either way
+    the caller keeps the tensors alive until the stream that reads them has
+    passed that point."""
     import torch
 
     out = _macros(d, device)
-    torch.cuda.synchronize(device)
+    cur = torch.cuda.current_stream(device)
+    if stream is None:
+        cur.synchronize()
+    else:
+        torch.cuda.ExternalStream(stream, device=device).wait_stream(cur)
     return out
 
 
