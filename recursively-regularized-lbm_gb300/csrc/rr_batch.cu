@@ -617,8 +617,7 @@ rr_status rr_set_stage(rr_solver *s, int method, int rows, int stages) {
         if (rows < 1 || rows > rmax || stages < 2 || stages > 4)
             return rr_internal_error(RR_ERR_INVALID, "rows = %d (1 .. %d), stages = %d (2 .. 4)", rows, rmax, stages);
         const size_t wall = s->p.face[0] != RR_FACE_PERIODIC ? (size_t)stages * 2 * s->p.q * rows * s->ops->elem_bytes : 0;
-        // input and output stages, the x-wall gather
-        const size_t smem = 128 + 2 * (size_t)stages * s->p.q * rows * s->p.lx * s->ops->elem_bytes + wall;
+        const size_t smem = 128 + (size_t)stages * s->p.q * rows * s->p.lx * s->ops->elem_bytes + wall;
         if (smem > 227 * 1024)
             return rr_internal_error(RR_ERR_INVALID, "%d stages of %d rows need %zu bytes of shared memory (> 227 KB)",
                                      stages, rows, smem);

@@ -90,37 +90,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
-// bytes (a multiple of 16) from shared src to global dst, in the thread's
-// current bulk group
-__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// until at most n of the thread's bulk groups still read shared memory
-__device__ __forceinline__ void bulk_wait_read(uint32_t n) {
-    switch (n) {
-    case 0: asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); break;
-    case 1: asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); break;
-    case 2: asm volatile("cp.async.bulk.wait_group.read 2;" ::: "memory"); break;
-    default: asm volatile("cp.async.bulk.wait_group.read 3;" ::: "memory"); break;
-    }
-}
-// until every bulk group of the thread has completed
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
-// the compute warps' own barrier (named barrier 1), with the AND of `ok`
-__device__ __forceinline__ bool compute_bar_and(int ok) {
-    int r;
-    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, 1, 256, p;\n\t"
-                 "selp.s32 %0, 1, 0, q;\n\t}"
-                 : "=r"(r)
-                 : "r"(ok)
-                 : "memory");
-    return r != 0;
-}
-__device__ __forceinline__ void compute_bar() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
-
 // first row and row count of block b
 __device__ __forceinline__ void stage_block(uint32_t b, const FastDiv &div_yblocks, uint32_t yblocks, uint32_t R,
                                             int ny, int &z, int &y0, int &rows) {
@@ -137,16 +106,9 @@ constexpr int STAGE_THREADS = STAGE_CONSUMERS + 32;    // + the producer warp
 // of the CTA's blocks it waits until the 8 compute warps have released the
 // stage (empty barrier, one arrive per warp), then issues the block's bulk
 // copies onto the stage's full barrier.  The compute warps wait on the full
-// barrier, compute into the block's output stage in shared memory and
-// release the input stage; thread 0 then writes the output stage's rows out
-// with one bulk copy per population (the block's rows are consecutive in
-// memory), so no population leaves in per-thread 16-bit stores.  The compute
-// warps meet twice per block at a barrier of their own: before writing an
-// output stage (whose previous bulk stores thread 0 has waited to be read)
-// and before its bulk stores; a wait that gave up in any warp stops them all
-// at the first.
+// barrier, compute, and release the stage; no barrier over the whole CTA.
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(STAGE_THREADS, 2) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
+__global__ void __launch_bounds__(STAGE_THREADS, 3) stage_kernel(const __grid_constant__ StageArgs<LT::Q, S> a) {
     using T = typename CType<S>::T;
     extern __shared__ __align__(128) unsigned char stage_smem[];
     uint64_t *full = reinterpret_cast<uint64_t *>(stage_smem);  // [STAGE_MAX]
@@ -160,8 +122,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) stage_kernel(const __grid_co
     // (their own post-collision populations), gathered per stage by the
     // producer warp: wall[s][side][i][r] = f_opp(i) of row r's node on that side
     const bool xwall = g.face[0] != FACE_PERIODIC;
-    S *outb = buf + (size_t)NS * a.stage_elems; // the output stages
-    S *wall = outb + (size_t)NS * a.stage_elems;
+    S *wall = buf + (size_t)NS * a.stage_elems;
     const uint32_t wall_elems = 2u * (uint32_t)LT::Q * R;
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < NS; s++) {
@@ -236,18 +197,13 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) stage_kernel(const __grid_co
     }
     const T Fx = T(a.F[0]), Fy = T(a.F[1]), Fz = T(a.F[2]);
     for (uint32_t k = 0; k < mine; k++) {
-        // the output stage of this block is free once the bulk stores of
-        // block k - NS have read it
-        if (threadIdx.x == 0 && k >= NS) bulk_wait_read(NS - 1);
-        const bool ok = mbar_wait(&full[k % NS], (k / NS) & 1u, a.wait_limit);
-        if (!compute_bar_and(ok)) {
-            if (!ok && (threadIdx.x & 31u) == 0) atomicOr(a.status, WATCH_STAGE_WAIT);
+        if (!mbar_wait(&full[k % NS], (k / NS) & 1u, a.wait_limit)) {
+            if ((threadIdx.x & 31u) == 0) atomicOr(a.status, WATCH_STAGE_WAIT);
             break;
         }
         int z, y0, rows;
         stage_block(blockIdx.x + k * gridDim.x, a.div_yblocks, a.yblocks, R, g.ny, z, y0, rows);
         const S *st = buf + (size_t)(k % NS) * a.stage_elems;
-        S *ot = outb + (size_t)(k % NS) * a.stage_elems;
         const S *wb = wall + (size_t)(k % NS) * wall_elems;
         // the main loop takes every node of the block's rows, or with x walls
         // the x in [1, nx-2] ones; the x-wall nodes go to two warps of their own
@@ -270,7 +226,6 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) stage_kernel(const __grid_co
             const int y = y0 + r;
             const uint32_t idx = ((uint32_t)z * (uint32_t)g.ny + (uint32_t)y) * (uint32_t)nx + (uint32_t)x;
             const S *row = st + (size_t)r * nx;
-            S *orow = ot + (size_t)r * nx + x; // this node's place in the output stage (population 0)
             T d[LT::Q];
             if (x >= 1 && x <= nx - 2) {
                 static_for<LT::Q>([&](auto ic) {
@@ -314,36 +269,19 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) stage_kernel(const __grid_co
             collide<LT, T, FORCE>(d, m, m.drho, ux, uy, uz, T(a.om1), Fx, Fy, Fz);
             if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
                 if (g.sround) {
-                    store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux),
-                                             [&](int i) { return orow + (size_t)i * R * nx; });
+                    store_sr_pairs<LT, S, T>(d, sr_seed(idx, m.drho, ux), [&](int i) { return a.dst[i] + idx; });
                     continue;
                 }
             }
             static_for<LT::Q>([&](auto ic) {
                 constexpr int i = decltype(ic)::value;
-                st_dev<T>(orow + (size_t)i * R * nx, d[i]);
+                st_dev<T>(a.dst[i] + idx, d[i]);
             });
         }
-        // this warp is done with input stage k % NS
+        // this warp is done with stage k % NS
         __syncwarp();
         if ((threadIdx.x & 31u) == 0) mbar_arrive(&empty[k % NS]);
-        // the output stage complete (its writes visible to the bulk copies),
-        // thread 0 writes the block's rows out: population i of rows y0 ..
-        // y0 + rows - 1 of plane z is one run of rows nx values
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        compute_bar();
-        if (threadIdx.x == 0) {
-            const uint32_t bytes = (uint32_t)rows * (uint32_t)nx * (uint32_t)sizeof(S);
-            const size_t row0 = ((size_t)z * (size_t)g.ny + (size_t)y0) * (size_t)nx;
-            static_for<LT::Q>([&](auto ic) {
-                constexpr int i = decltype(ic)::value;
-                bulk_s2g(a.dst[i] + row0, ot + (size_t)i * R * nx, bytes);
-            });
-            bulk_commit();
-        }
     }
-    // the CTA leaves once its bulk stores have completed
-    if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // rows on a y or z face (any kind): 32 consecutive nodes of one row per warp
