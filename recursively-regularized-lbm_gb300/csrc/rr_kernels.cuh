@@ -367,18 +367,21 @@ __device__ __noinline__ void wall_multi(const S *__restrict__ fin, const Geom &g
 // resident CTAs per SM the tile step is compiled for (register budget 65536 /
 // (256 x that)).  The packed-pair form of the DNS step (PAIRS: two nodes'
 // populations live per thread) runs FP16/BF16 at 3 CTAs, 80 registers (at 2
-// CTAs, 128 registers, 2 % slower), FP32 at 2 (its pairs of FP32 loads take
-// twice the registers).  One node per thread: the force-free DNS step at 5
+// CTAs, 128 registers, 2 % slower), FP32 and the forced step at 2 (FP32
+// pairs take twice the registers for their loads; the forced collision at 80
+// registers spills: channel 0.44 ms per step against 0.355 at 2 CTAs).  One node per thread: the force-free DNS step at 5
 // (48 registers), the forced one and the trip-forcing step at 4, the WALE
 // passes and the BGK step at 5.
 #ifndef RR_WALE_MIN_BLOCKS
 #define RR_WALE_MIN_BLOCKS 5
 #endif
-template <typename S> __host__ __device__ constexpr int pair_min_blocks() { return sizeof(S) == 2 ? 3 : 2; }
+template <typename S, bool FORCE = false> __host__ __device__ constexpr int pair_min_blocks() {
+    return (sizeof(S) == 2 && !FORCE) ? 3 : 2;
+}
 template <typename S, bool FORCE = false, int MODE = 0, bool FIELD = false, bool BGK = false, bool PAIRS = false>
 constexpr int tile_min_blocks() {
     return sizeof(S) == 8 ? 2
-           : PAIRS        ? pair_min_blocks<S>()
+           : PAIRS        ? pair_min_blocks<S, FORCE>()
            : MODE != 0    ? RR_WALE_MIN_BLOCKS
            : FIELD        ? 4
            : BGK          ? 5
@@ -387,7 +390,9 @@ constexpr int tile_min_blocks() {
 }
 // the batch kernel holds its loop state and the shared descriptor on top of
 // the tile step's registers
-template <typename S> constexpr int batch_min_blocks() { return sizeof(S) == 8 ? 2 : pair_min_blocks<S>(); }
+template <typename S, bool FORCE = false> constexpr int batch_min_blocks() {
+    return sizeof(S) == 8 ? 2 : pair_min_blocks<S, FORCE>();
+}
 
 template <typename T> __device__ __forceinline__ T rr_sqrt(T v);
 template <> __device__ __forceinline__ float rr_sqrt(float v) { return sqrtf(v); }
@@ -762,7 +767,7 @@ struct BatchArgs {
 };
 
 template <class LT, typename S, bool FORCE>
-__global__ void __launch_bounds__(256, batch_min_blocks<S>()) batch_kernel(const __grid_constant__ BatchArgs<LT::Q, S> b) {
+__global__ void __launch_bounds__(256, batch_min_blocks<S, FORCE>()) batch_kernel(const __grid_constant__ BatchArgs<LT::Q, S> b) {
     using TA = TileArgs<LT::Q, S>;
     static_assert(sizeof(TA) % 8 == 0, "descriptor copy is by 8-byte words");
     __shared__ __align__(16) unsigned long long sdesc[sizeof(TA) / 8];
