@@ -62,6 +62,7 @@ WORKLOADS = {
     "channel_les_fdbc_f16": dict(kind="channel", storage="f16", fdbc=True),
     "tg100_f64": dict(kind="tg", storage="f64"),
     "tg128_f16": dict(kind="tg128", storage="f16"),
+    "tg128_f32": dict(kind="tg128", storage="f32"),
     "tg128_bgk_f16": dict(kind="tg128", storage="f16", bgk=True),
 }
 BYTES_PER_POP = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}

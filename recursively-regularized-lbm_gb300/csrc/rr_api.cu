@@ -659,6 +659,7 @@ rr_status rr_destroy(rr_solver *s) {
         cudaStreamDestroy(s->side);
     }
     if (s->fork) cudaEventDestroy(s->fork);
+    if (s->copied) cudaEventDestroy(s->copied);
     if (s->join) cudaEventDestroy(s->join);
     if (s->home) cudaStreamDestroy(s->home);
     cudaGetLastError();
@@ -689,6 +690,11 @@ rr_status init_state_at(rr_solver *s, const double *f, const double *rho, const 
     for (int k = 0; k < 4 && e == cudaSuccess; k++)
         e = cudaMemcpyAsync(dst[k], src[k], n * sizeof(double), kind, s->stream);
     if (e == cudaSuccess && f) e = cudaMemcpyAsync(d_f, f, nf * sizeof(double), kind, s->stream);
+    // host buffers: the call returns once they are copied (the upload runs on)
+    if (e == cudaSuccess && where == RR_HOST) {
+        if (!s->copied) e = cudaEventCreateWithFlags(&s->copied, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(s->copied, s->stream);
+    }
     // the reference's first step computes tau_t from these macros (main.cu:375-379)
     if (e == cudaSuccess && s->p.use_les) e = rr::launch_wale(s->g, s->p.cw, d_ux, d_uy, d_uz, d_tt, s->stream);
     // the trip forcing restarts with the run: srand(12345), phase 0; the
@@ -723,7 +729,7 @@ rr_status init_state_at(rr_solver *s, const double *f, const double *rho, const 
     s->ready = true;
     s->stepped = false;
     RR_CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
-    if (where == RR_HOST) RR_CK(cudaStreamSynchronize(s->stream));
+    if (where == RR_HOST) RR_CK(cudaEventSynchronize(s->copied));
     return RR_OK;
 }
 

@@ -75,6 +75,7 @@ struct rr_solver {
     uint32_t nfrows = 0;
     cudaStream_t side = nullptr;     // staged step: the face-row launch, beside the interior one
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t copied = nullptr;    // rr_init_state from host buffers: the copies are done
     double *ffield = nullptr;        // trip forcing: the force fields of two steps (2 x 3 arrays of g.stride)
     TripRand trip_rng;
     double trip_phase = 0.0;

@@ -578,88 +578,181 @@ __device__ __forceinline__ void tile_node(const A &a, uint32_t row, int x, int y
     });
 }
 
-// Stores two nodes' populations (ia: the low lane's node, ib the high
-// lane's: x-adjacent nodes at an odd and an even element, or the two x ends
-// of a periodic row; every store is a 16- or 32-bit scalar store).  With
-// stochastic rounding each node draws from its own stream exactly as
-// store_sr_pairs does for a node alone: per population pair (i0, i1) one LCG
-// draw r, folded f = r ^ (r >> 16), whose low half rounds i0 and high half
-// i1; one packed conversion rounds population i of both nodes, the first
-// node's bits in the low half of the random operand, the second's in the high.
+// Stores the populations of two x-adjacent nodes ia, ia + 1 (ia even): one
+// aligned word per population (32 bits for FP16/BF16, 64 for FP32), whole
+// sectors across the warp; keep (put_word) drops a node that another work
+// item owns.  With stochastic rounding each node draws from its own stream
+// exactly as store_sr_pairs does for a node alone: per population pair
+// (i0, i1) one LCG draw r, folded f = r ^ (r >> 16), whose low half rounds i0
+// and high half i1; one packed conversion rounds population i of both nodes,
+// the first node's bits in the low half of the random operand, the second's
+// in the high.
 template <class LT, typename S>
-__device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, uint32_t ib, const F2 (&d)[LT::Q],
-                                           bool sround, uint32_t sa, uint32_t sb) {
+__device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, const F2 (&d)[LT::Q], bool sround,
+                                           uint32_t sa, uint32_t sb, uint32_t keep = 3u) {
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (sround) {
             uint32_t ra = sa, rb = sb;
-            auto put = [&](S *p, uint32_t w) {
-                *reinterpret_cast<unsigned short *>(p + ia) = (unsigned short)(w & 0xFFFFu);
-                *reinterpret_cast<unsigned short *>(p + ib) = (unsigned short)(w >> 16);
-            };
             static_for<(LT::Q + 1) / 2>([&](auto jc) {
                 constexpr int i0 = 2 * decltype(jc)::value, i1 = i0 + 1;
                 ra = ra * 1664525u + 1013904223u;
                 rb = rb * 1664525u + 1013904223u;
                 const uint32_t fa = ra ^ (ra >> 16), fb = rb ^ (rb >> 16);
-                put(dst[i0], cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)));
+                put_word<S>(dst[i0] + ia, cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)), keep);
                 if constexpr (i1 < LT::Q)
-                    put(dst[i1], cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)));
+                    put_word<S>(dst[i1] + ia, cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)), keep);
             });
             return;
         }
     }
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        st_dev<float>(dst[i] + ia, d[i].lo());
-        st_dev<float>(dst[i] + ib, d[i].hi());
+        put_word<S>(dst[i] + ia, word_of<S>(d[i]), keep);
     });
 }
 
-// Two x-adjacent nodes idx, idx + 1 of a fast row (idx at an odd x) in packed
-// FP32 pairs.  A population with c_x != 0 streams in from x - c_x, an even
-// element offset for both nodes together: one 32-bit (16-bit storage) or
-// 64-bit (FP32) load; the c_x = 0 populations take two scalar loads.  The
-// arithmetic is the scalar node's, lane by lane.
-// the DNS step of the node pair ia (low lane), ib (high lane) from its
-// post-stream populations d: moments, the watchdog, the collision, the stores
+// the DNS step of the node pair ia, ia + 1 from its post-stream populations
+// d: moments, the watchdog, the collision, the stores (of the nodes in keep)
 template <class LT, typename S, bool FORCE>
-__device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, uint32_t ib, S *const *dst, double om1_,
-                                          const double *Fv, int *status, bool sround) {
+__device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, S *const *dst, double om1_, const double *Fv,
+                                          int *status, bool sround, uint32_t keep) {
     const F2 Fx(Fv[0]), Fy(Fv[1]), Fz(Fv[2]);
     Mom<F2> m = moments<LT>(d);
     F2 ux, uy, uz;
     velocity(m, Fx, Fy, Fz, ux, uy, uz);
-    if (!(m.drho.lo() > -0.9f && m.drho.lo() < 9.0f && m.drho.hi() > -0.9f && m.drho.hi() < 9.0f))
-        atomicOr(status, 1);
+    const bool ok_lo = m.drho.lo() > -0.9f && m.drho.lo() < 9.0f, ok_hi = m.drho.hi() > -0.9f && m.drho.hi() < 9.0f;
+    if (((keep & 1u) && !ok_lo) || ((keep & 2u) && !ok_hi)) atomicOr(status, 1);
     collide<LT, F2, FORCE>(d, m, m.drho, ux, uy, uz, F2(om1_), Fx, Fy, Fz);
-    store_pair<LT, S>(dst, ia, ib, d, sround, sr_seed(ia, m.drho.lo(), ux.lo()), sr_seed(ib, m.drho.hi(), ux.hi()));
+    store_pair<LT, S>(dst, ia, d, sround, sr_seed(ia, m.drho.lo(), ux.lo()), sr_seed(ia + 1u, m.drho.hi(), ux.hi()),
+                      keep);
 }
 
+// Two x-adjacent nodes x, x + 1 (x even) of a row off every y/z face.  The
+// warp holds the 64-node segment [x0, x0 + 64) of the row (x0 a multiple of
+// 64; lanes past the row's end load nothing and store nothing).  Each
+// population is one aligned word load from its upstream row, whole sectors
+// across the warp; a population with c_x = +1 takes the element below its
+// word from the lane below by a shuffle, c_x = -1 the element above from the
+// lane above, and the segment's first (c_x = +1) and last (c_x = -1) lane load
+// their missing element alone, wrapped periodically in x.  Every lane of the
+// warp must call this (the shuffles take all 32).  The pair is collided in
+// packed FP32 (pair_core), bit for bit the scalar node arithmetic.  xends:
+// the x = 0 and x = nx-1 nodes (x walls) belong to the x-face items; the lanes
+// holding them compute their pair (the wall node from wrapped values) and
+// store only the other node.
 template <class LT, typename S, bool FORCE, class A>
-__device__ __forceinline__ void pair_node(const A &a, uint32_t idx) {
+__device__ __forceinline__ void pair_row(const A &a, uint32_t row, int x0, uint32_t lane, bool xends) {
+    using W = typename PairWord<S>::W;
+    const Geom &g = a.g;
+    const int nx = g.nx;
+    const int x = x0 + 2 * (int)lane;
+    const bool active = x < nx;
+    const uint32_t rbase = row * (uint32_t)nx;
+    const bool last = active && (x + 2 >= nx || lane == 31u);
+    const int xlo = x0 == 0 ? nx - 1 : x0 - 1; // the first lane's element at x - 1
+    const int xhi = x + 2 >= nx ? 0 : x + 2;   // the last lane's element at x + 2
     F2 d[LT::Q];
-    static_for<LT::Q>([&](auto ic) {
-        constexpr int i = decltype(ic)::value;
-        const S *p = a.src[i] + idx; // the upstream value of node idx
-        if constexpr (LT::cx(i) == 0) d[i] = F2(ld_dev<float>(p), ld_dev<float>(p + 1));
-        else d[i] = ld_pair<S>(p);
-    });
-    pair_core<LT, S, FORCE>(d, idx, idx + 1u, a.dst, a.om1, a.F, a.status, a.g.sround != 0);
+    if constexpr (sizeof(S) == 4) {
+        // FP32 words (64 bits): every load first (the words and the end
+        // lanes' missing elements), then the shuffles, so that all loads are
+        // in flight together (interleaved, the shuffles held them back:
+        // cavity 128^3 153 us against 100 us per step)
+        W w[LT::Q], e[LT::Q];
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int cx = LT::cx(i);
+            // element 0 of the upstream row of population i
+            const S *up = a.src[i] + (rbase + (uint32_t)cx);
+            w[i] = active ? ld_word<S>(up + x) : W(0);
+            if constexpr (cx == 1) e[i] = lane == 0u ? elem_hi<S>(up + xlo) : W(0);
+            if constexpr (cx == -1) e[i] = last ? elem_lo<S>(up + xhi) : W(0);
+        });
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int cx = LT::cx(i);
+            W v = w[i];
+            if constexpr (cx == 1) {
+                const W b = __shfl_up_sync(0xFFFFFFFFu, v, 1);
+                v = join_word<S>(lane == 0u ? e[i] : b, v);
+            } else if constexpr (cx == -1) {
+                const W b = __shfl_down_sync(0xFFFFFFFFu, v, 1);
+                v = join_word<S>(v, last ? e[i] : b);
+            }
+            d[i] = word_f2<S>(v);
+        });
+    } else {
+        // 16-bit words: population by population (loads first measured
+        // Taylor-Green 128^3 65 against 60 us per step)
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int cx = LT::cx(i);
+            // element 0 of the upstream row of population i
+            const S *up = a.src[i] + (rbase + (uint32_t)cx);
+            W w = active ? ld_word<S>(up + x) : W(0);
+            if constexpr (cx == 1) {
+                W b = __shfl_up_sync(0xFFFFFFFFu, w, 1);
+                if (lane == 0u) b = elem_hi<S>(up + xlo);
+                w = join_word<S>(b, w);
+            } else if constexpr (cx == -1) {
+                W b = __shfl_down_sync(0xFFFFFFFFu, w, 1);
+                if (last) b = elem_lo<S>(up + xhi);
+                w = join_word<S>(w, b);
+            }
+            d[i] = word_f2<S>(w);
+        });
+    }
+    if (!active) return;
+    const uint32_t keep = !xends ? 3u : x == 0 ? 2u : x + 2 == nx ? 1u : 3u;
+    pair_core<LT, S, FORCE>(d, rbase + (uint32_t)x, a.dst, a.om1, a.F, a.status, g.sround != 0, keep);
 }
 
-// The node(s) a lane of work item `item` takes: false if none.  The slow
-// items go first so that they overlap the bulk instead of forming a tail: the
-// edge items, then the rows of the last z plane (the row order is rotated by
-// one plane).  pair: the lane takes the node pair (x, x + 1).
-template <bool PAIRABLE, class A>
-__device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t lane, uint32_t &row, int &x,
-                                            int &y, int &z, bool &fast, bool &pair) {
-    pair = false;
+// A row item of the aligned pair layout, a 64-node segment of one row: false
+// for the other items (x-face and edge items, the one-node path's).  Without
+// x walls the segments cover every x and there are no other items; with x
+// walls the x = 0 and x = nx-1 nodes stay with the x-face and edge items.  A
+// row on a y/z face or a periodic edge row takes the general node path, each
+// lane its two nodes one after the other.
+template <class LT, typename S, bool FORCE, class A>
+__device__ __forceinline__ bool pair_item(const A &a, uint32_t item, uint32_t lane) {
+    if (item >= a.nitems) return true; // the whole warp: nothing
+    const Geom &g = a.g;
+    const uint32_t nedge_items = a.nitems - a.nmain;
+    if (item < nedge_items) return false;
+    const uint32_t mitem = item - nedge_items;
+    const uint32_t grp = fdiv(mitem, a.div_group);
+    const uint32_t sub = mitem - grp * a.group_items;
+    if (sub >= a.rows_group * a.segs) return false;
+    const uint32_t rl = fdiv(sub, a.div_segs);
+    uint32_t row = grp * a.rows_group + rl;
+    if (row >= a.nrows) return true; // the whole warp: nothing
+    row += a.rot;
+    if (row >= a.nrows) row -= a.nrows;
+    const int z = (int)fdiv(row, a.div_ny);
+    const int y = (int)(row - (uint32_t)z * (uint32_t)g.ny);
+    const int x0 = (int)(sub - rl * a.segs) * 64;
+    const bool xends = a.xf_half != 0;
+    if (y >= 1 && y <= g.ny - 2 && z >= 1 && z <= g.nz - 2) {
+        pair_row<LT, S, FORCE>(a, row, x0, lane, xends);
+        return true;
+    }
+    const int x = x0 + 2 * (int)lane;
+    if (x >= g.nx) return true;
+#pragma unroll 1
+    for (int k = 0; k < 2; k++)
+        if (!xends || (x + k != 0 && x + k != g.nx - 1))
+            tile_node<LT, S, FORCE, 0, false, false>(a, row, x + k, y, z, false);
+    return true;
+}
+
+// The node a lane of work item `item` takes in the one-node layout: false if
+// none.  The slow items go first so that they overlap the bulk instead of
+// forming a tail: the edge items, then the rows of the last z plane (the row
+// order is rotated by one plane).
+template <class A>
+__device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t lane, uint32_t &row, int &x, int &y,
+                                            int &z, bool &fast) {
     if (item >= a.nitems) return false;
     const Geom &g = a.g;
-    // the slow items go first so that they overlap the bulk instead of
-    // forming a tail: the edge items, then the rows of the last z plane (the
-    // row order is rotated by one plane)
     const uint32_t nedge_items = a.nitems - a.nmain;
     if (item >= nedge_items) {
         const uint32_t mitem = item - nedge_items;
@@ -669,11 +762,7 @@ __device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t 
         if (sub < a.rows_group * a.segs) {
             const uint32_t rl = fdiv(sub, a.div_segs);
             row = grp * a.rows_group + rl;
-            const uint32_t col = (sub - rl * a.segs) * 32u + lane;
-            pair = PAIRABLE && a.pairs != 0;
-            // pairs (1 + 2 col, 2 + 2 col): an even nx has an even number of
-            // interior nodes, so the pairs cover x in [1, nx-2] exactly
-            x = 1 + (int)(pair ? 2u * col : col);
+            x = 1 + (int)((sub - rl * a.segs) * 32u + lane);
             fast = true;
             if (x > g.nx - 2) return false;
         } else {
@@ -716,25 +805,18 @@ __device__ __forceinline__ bool tile_decode(const A &a, uint32_t item, uint32_t 
 template <class LT, typename S, bool FORCE, int MODE = 0, bool FIELD = false, bool BGK = false, bool PAIRS = true,
           class A>
 __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t lane) {
-    // the packed-pair form: 16- and 32-bit storage, the DNS step with a
+    // the aligned pair layout: 16- and 32-bit storage, the DNS step with a
     // uniform force and the RR collision (the host sets a.pairs only then,
     // and only for an even nx); PAIRS = false compiles it out
     constexpr bool PAIRABLE = PAIRS && sizeof(S) <= 4 && MODE == 0 && !FIELD && !BGK;
+    if constexpr (PAIRABLE) {
+        if (a.pairs && pair_item<LT, S, FORCE>(a, item, lane)) return;
+    }
     uint32_t row;
     int x, y, z;
-    bool fast, pair;
-    if (!tile_decode<PAIRABLE>(a, item, lane, row, x, y, z, fast, pair)) return;
-    if constexpr (PAIRABLE) {
-        if (pair && fast) {
-            pair_node<LT, S, FORCE>(a, row * (uint32_t)a.g.nx + (uint32_t)x);
-            return;
-        }
-    }
-    // a row on a y/z face or a periodic edge row in the pair layout: its two
-    // nodes one after the other through the general node path
-    const int nn = pair ? 2 : 1;
-#pragma unroll 1
-    for (int k = 0; k < nn; k++) tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x + k, y, z, fast);
+    bool fast;
+    if (!tile_decode(a, item, lane, row, x, y, z, fast)) return;
+    tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x, y, z, fast);
 }
 
 // PAIRS: the DNS step in the packed-pair layout (a.pairs set); else one node
@@ -798,8 +880,26 @@ __global__ void __launch_bounds__(256, batch_min_blocks<S, FORCE>()) batch_kerne
     }
 }
 
-// a readout's outputs of one node from its post-stream deviations d
-template <class LT, typename T>
+// 1 / r to within a few units of the last FP64 place: the FP32 reciprocal
+// refined by one Newton-Raphson step x' = x (2 - r x), which squares its
+// relative error (~6e-8 -> ~4e-15)
+__device__ __forceinline__ double recip_nr(double r) {
+    const double x = double(1.0f / float(r));
+    return x * fma(-r, x, 2.0);
+}
+
+// a readout's outputs of one node from its post-stream deviations d.
+// ACC selects the moment arithmetic:
+//   0: FP64 per population, w_i (1 + d_i) summed (macrovar.cu:18-28), for FP64 storage;
+//   1: FP64 sums of d_i per weight class k = |c_i|^2, rho = 1 + sum_k w_k s_k,
+//      j = sum_k w_k (signed class sums), for 32-bit storage (the same sums,
+//      reassociated: the w_i of opposite populations cancel exactly);
+//   2: as 1 with the class sums in FP32 and rho - 1, j, u in FP32, for 16-bit
+//      storage, whose values FP32 holds exactly (11 or 8 significant bits): the
+//      FP32 rounding of the sums (~1e-7 relative) is far below the storage's.
+// FP64 throughput on this part is a small fraction of FP32: modes 1 and 2 keep the
+// readout of a narrow state memory-bound.
+template <class LT, typename T, int ACC = 0>
 __device__ __forceinline__ void readout_node(const T (&d)[LT::Q], uint32_t idx, bool bgk, double Fx_, double Fy_,
                                              double Fz_, double *__restrict__ fo, unsigned long long fo_stride,
                                              const int *__restrict__ pos, double *__restrict__ rho,
@@ -810,6 +910,54 @@ __device__ __forceinline__ void readout_node(const T (&d)[LT::Q], uint32_t idx, 
             constexpr int i = decltype(ic)::value;
             fo[(unsigned long long)pos[i] * fo_stride + idx] = LT::w(i) * (1.0 + double(d[i]));
         });
+    }
+    if constexpr (ACC != 0) {
+        if (!rho) return;
+        using A = typename std::conditional<ACC == 2, float, double>::type;
+        A s[4] = {}, sx[4] = {}, sy[4] = {}, sz[4] = {};
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            constexpr int k = LT::nnz(i);
+            const A v = A(d[i]);
+            s[k] += v;
+            if constexpr (LT::cx(i) > 0) sx[k] += v;
+            if constexpr (LT::cx(i) < 0) sx[k] -= v;
+            if constexpr (LT::cy(i) > 0) sy[k] += v;
+            if constexpr (LT::cy(i) < 0) sy[k] -= v;
+            if constexpr (LT::cz(i) > 0) sz[k] += v;
+            if constexpr (LT::cz(i) < 0) sz[k] -= v;
+        });
+        constexpr int NK = LT::Q == 27 ? 4 : 3;
+        A dr = A(LT::Set::weight_of(0)) * s[0], jx = 0, jy = 0, jz = 0;
+#pragma unroll
+        for (int k = 1; k < NK; k++) {
+            const A wk = A(LT::Set::weight_of(k));
+            dr += wk * s[k];
+            jx += wk * sx[k];
+            jy += wk * sy[k];
+            jz += wk * sz[k];
+        }
+        const double r = 1.0 + double(dr);
+        rho[idx] = r;
+        jx += A(0.5 * Fx_);
+        jy += A(0.5 * Fy_);
+        jz += A(0.5 * Fz_);
+        if (bgk) { // the incompressible velocity, not divided by rho
+            ux_o[idx] = double(jx);
+            uy_o[idx] = double(jy);
+            uz_o[idx] = double(jz);
+        } else if constexpr (ACC == 2) {
+            const float ri = 1.0f / (1.0f + float(dr));
+            ux_o[idx] = double(jx * ri);
+            uy_o[idx] = double(jy * ri);
+            uz_o[idx] = double(jz * ri);
+        } else {
+            const double ri = recip_nr(r);
+            ux_o[idx] = jx * ri;
+            uy_o[idx] = jy * ri;
+            uz_o[idx] = jz * ri;
+        }
+        return;
     }
     if (rho) {
         // moments in FP64 from the stored state (macrovar.cu:18-28)
@@ -857,7 +1005,8 @@ readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double
     pull<LT>(fin, g.stride, g.nx, g.ny, g.nz, x, y, z, d);
     const T Fx = T(Fx_), Fy = T(Fy_), Fz = T(Fz_);
     if (g.wallmask && any_wall(x, y, z, g)) wall_pass<LT, S, T, FORCE>(fin, g, idx, x, y, z, d, Fx, Fy, Fz);
-    readout_node<LT, T>(d, idx, g.bgk != 0, Fx_, Fy_, Fz_, fo, fo_stride, pos, rho, ux_o, uy_o, uz_o);
+    readout_node<LT, T, sizeof(S) == 8 ? 0 : sizeof(S) == 4 ? 1 : 2>(d, idx, g.bgk != 0, Fx_, Fy_, Fz_, fo,
+                                                                      fo_stride, pos, rho, ux_o, uy_o, uz_o);
 }
 
 // State upload: populations in the reference's post-stream form (FP64,
@@ -866,7 +1015,7 @@ readout_kernel(const S *__restrict__ fin, Geom g, double Fx_, double Fy_, double
 // are not the moments of f).  Collides and writes the post-collision state.
 template <class LT, typename S, bool FORCE>
 __global__ void __launch_bounds__(256)
-upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, double Fz_,
+upload_kernel(S *__restrict__ fout, Geom g, double tau, double omc, double Fx_, double Fy_, double Fz_,
               const double *__restrict__ fi, unsigned long long fi_stride, const int *__restrict__ pos,
               const double *__restrict__ rho, const double *__restrict__ ux,
               const double *__restrict__ uy, const double *__restrict__ uz,
@@ -886,6 +1035,18 @@ upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, 
             constexpr int i = decltype(ic)::value;
             d[i] = T(fi[(unsigned long long)pos[i] * fi_stride + idx] / LT::w(i) - 1.0);
         });
+    } else if constexpr (sizeof(S) < 8) {
+        // the equilibrium below in FP32 arithmetic for 16/32-bit storage (the
+        // result is rounded to the storage type; FP64 throughput is a small
+        // fraction of FP32 on this part)
+        const float dr = float(rho[idx] - 1.0), r = float(rho[idx]);
+        const float u0 = float(ux[idx]), u1 = float(uy[idx]), u2 = float(uz[idx]);
+        const float uv = 3.0f * (u0 * u0 + u1 * u1 + u2 * u2);
+        static_for<LT::Q>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            const float eu = 3.0f * (float(LT::cx(i)) * u0 + float(LT::cy(i)) * u1 + float(LT::cz(i)) * u2);
+            d[i] = dr + r * (eu + 0.5f * (eu * eu - uv));
+        });
     } else {
         // second-order equilibrium of (rho, u), Cavity/collision.f90:103-114:
         // feq = w rho (1 + eu + (eu^2 - uv)/2), eu = c.u / cs^2, uv = u.u / cs^2
@@ -898,13 +1059,15 @@ upload_kernel(S *__restrict__ fout, Geom g, double tau, double Fx_, double Fy_, 
         });
     }
     Mom<T> m = moments<LT>(d);
-    const double tau_eff = taut ? tau + taut[idx] : tau;
+    // relaxation factor (BGK 1 / tau, RR 1 - 1 / tau): the host's omc unless
+    // tau_t varies per node
+    const double om = !taut ? omc : g.bgk ? 1.0 / (tau + taut[idx]) : 1.0 - 1.0 / (tau + taut[idx]);
     if (g.bgk)
-        collide_bgk<LT, T, FORCE>(d, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]), T(1.0 / tau_eff),
-                                  T(Fx_), T(Fy_), T(Fz_));
+        collide_bgk<LT, T, FORCE>(d, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]), T(om), T(Fx_), T(Fy_),
+                                  T(Fz_));
     else
-        collide<LT, T, FORCE>(d, m, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]),
-                              T(1.0 - 1.0 / tau_eff), T(Fx_), T(Fy_), T(Fz_));
+        collide<LT, T, FORCE>(d, m, T(rho[idx] - 1.0), T(ux[idx]), T(uy[idx]), T(uz[idx]), T(om), T(Fx_), T(Fy_),
+                              T(Fz_));
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
         st_dev<T>(fout + (unsigned long long)i * g.stride + idx, d[i]);

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 namespace rr {
 
@@ -62,6 +63,59 @@ template <> __device__ __forceinline__ F2 ld_pair(const __half *p) {
 }
 template <> __device__ __forceinline__ F2 ld_pair(const __nv_bfloat16 *p) {
     return F2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(p)));
+}
+
+// Two consecutive stored elements (the first at an even element offset) as
+// raw bits, the first element in the low half: 32 bits for FP16/BF16, 64 for
+// FP32.  The aligned pair layout moves populations between lanes in this form.
+template <typename S> struct PairWord { using W = uint32_t; };
+template <> struct PairWord<float> { using W = unsigned long long; };
+
+template <typename S> __device__ __forceinline__ typename PairWord<S>::W ld_word(const S *p) {
+    return *reinterpret_cast<const typename PairWord<S>::W *>(p);
+}
+// one element into the low / the high half of a word
+template <typename S> __device__ __forceinline__ typename PairWord<S>::W elem_lo(const S *p) {
+    if constexpr (sizeof(S) == 2) return (uint32_t)*reinterpret_cast<const unsigned short *>(p);
+    else return (unsigned long long)*reinterpret_cast<const uint32_t *>(p);
+}
+template <typename S> __device__ __forceinline__ typename PairWord<S>::W elem_hi(const S *p) {
+    if constexpr (sizeof(S) == 2) return (uint32_t)*reinterpret_cast<const unsigned short *>(p) << 16;
+    else return (unsigned long long)*reinterpret_cast<const uint32_t *>(p) << 32;
+}
+// (a's high element, b's low element): with a = (x-2, x-1), b = (x, x+1)
+// the elements at x-1 and x
+template <typename S>
+__device__ __forceinline__ typename PairWord<S>::W join_word(typename PairWord<S>::W a, typename PairWord<S>::W b) {
+    if constexpr (sizeof(S) == 2) return __byte_perm(a, b, 0x5432);
+    else return (a >> 32) | (b << 32);
+}
+// the word's elements as FP32 (exact conversions, as ld_dev's)
+template <typename S> __device__ __forceinline__ F2 word_f2(typename PairWord<S>::W w) {
+    if constexpr (std::is_same<S, __half>::value) return F2(__half22float2(*reinterpret_cast<const __half2 *>(&w)));
+    else if constexpr (std::is_same<S, __nv_bfloat16>::value)
+        return F2(__bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w)));
+    else return F2(*reinterpret_cast<const float2 *>(&w));
+}
+// an FP32 pair as a word of the storage type, each element rounded to nearest
+template <typename S> __device__ __forceinline__ typename PairWord<S>::W word_of(F2 v) {
+    typename PairWord<S>::W w;
+    if constexpr (std::is_same<S, __half>::value) *reinterpret_cast<__half2 *>(&w) = __float22half2_rn(v.v);
+    else if constexpr (std::is_same<S, __nv_bfloat16>::value)
+        *reinterpret_cast<__nv_bfloat162 *>(&w) = __float22bfloat162_rn(v.v);
+    else *reinterpret_cast<float2 *>(&w) = v.v;
+    return w;
+}
+// a word into two consecutive elements (the first at an even element
+// offset): keep = 3 both (one aligned store), 1 the first only, 2 the second
+// only
+template <typename S> __device__ __forceinline__ void put_word(S *p, typename PairWord<S>::W w, uint32_t keep) {
+    using W = typename PairWord<S>::W;
+    using E = typename std::conditional<sizeof(S) == 2, unsigned short, uint32_t>::type;
+    constexpr int SH = 8 * (int)sizeof(S);
+    if (keep == 3u) *reinterpret_cast<W *>(p) = w;
+    else if (keep == 1u) *reinterpret_cast<E *>(p) = (E)w;
+    else *reinterpret_cast<E *>(p + 1) = (E)(w >> SH);
 }
 
 } // namespace rr

@@ -1,8 +1,8 @@
 // pair_check.cu -- the packed FP32-pair node arithmetic (csrc/rr_pair.cuh)
 // against the scalar FP32 node arithmetic on the GPU, bit for bit: moments,
 // velocity, the second- and third-order coefficients, the full collision
-// (force-free and forced, D3Q27) and the stochastically rounded 16-bit stores,
-// for 65,536 random node pairs.  Built with
+// (force-free and forced, D3Q27) and the 16-bit stores of a pair as aligned
+// words (stochastic and nearest rounding), for 65,536 random node pairs.  Built with
 // the library's flags and run by tests/test_gpu_pair.py; prints the mismatch
 // bits (0: none) and exits 1 on a mismatch.
 #include <cstdio>
@@ -67,7 +67,7 @@ __global__ void check_store(int *bad, int n, S *a, S *b) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const unsigned long long stride = 2ull * n;
-    const uint32_t idx = 2u * t + 1u; // the pair's first node (odd), as in the steps
+    const uint32_t idx = 2u * t; // the pair's first node (even, aligned), as in the steps
     float da[27], db[27];
     F2 d2[27];
     for (int i = 0; i < 27; i++) {
@@ -76,17 +76,46 @@ __global__ void check_store(int *bad, int n, S *a, S *b) {
         d2[i] = F2(da[i], db[i]);
     }
     const uint32_t sa = mix32(idx * 7u + 1u), sb = mix32(idx * 7u + 8u);
-    store_sr_pairs<L27, S, float>(da, sa, [&](int i) { return a + i * stride + idx - 1; });
-    store_sr_pairs<L27, S, float>(db, sb, [&](int i) { return a + i * stride + idx; });
+    store_sr_pairs<L27, S, float>(da, sa, [&](int i) { return a + i * stride + idx; });
+    store_sr_pairs<L27, S, float>(db, sb, [&](int i) { return a + i * stride + idx + 1; });
     S *dst[27];
-    for (int i = 0; i < 27; i++) dst[i] = b + i * stride - 1;
-    store_pair<L27, S>(dst, idx, idx + 1u, d2, true, sa, sb);
+    for (int i = 0; i < 27; i++) dst[i] = b + i * stride;
+    store_pair<L27, S>(dst, idx, d2, true, sa, sb);
     for (int i = 0; i < 27; i++)
         for (int k = 0; k < 2; k++) {
-            const unsigned short x = *reinterpret_cast<unsigned short *>(a + i * stride + idx - 1 + k);
-            const unsigned short y = *reinterpret_cast<unsigned short *>(b + i * stride + idx - 1 + k);
+            const unsigned short x = *reinterpret_cast<unsigned short *>(a + i * stride + idx + k);
+            const unsigned short y = *reinterpret_cast<unsigned short *>(b + i * stride + idx + k);
             if (x != y) atomicOr(bad, 128);
         }
+    // nearest rounding: one word per population against two element stores
+    S *dn[27];
+    for (int i = 0; i < 27; i++) dn[i] = b + i * stride;
+    store_pair<L27, S>(dn, idx, d2, false, 0u, 0u);
+    for (int i = 0; i < 27; i++) {
+        const S ea = (S)da[i], eb = (S)db[i];
+        const unsigned short x0 = *reinterpret_cast<const unsigned short *>(&ea);
+        const unsigned short x1 = *reinterpret_cast<const unsigned short *>(&eb);
+        const unsigned short y0 = *reinterpret_cast<unsigned short *>(b + i * stride + idx);
+        const unsigned short y1 = *reinterpret_cast<unsigned short *>(b + i * stride + idx + 1);
+        if (x0 != y0 || x1 != y1) atomicOr(bad, 256);
+    }
+    // one node of the pair only (keep 1: the first, 2: the second): the other
+    // element keeps what was there
+    for (int keep = 1; keep <= 2; keep++) {
+        for (int i = 0; i < 27; i++) {
+            *reinterpret_cast<unsigned short *>(b + i * stride + idx) = 0x7777u;
+            *reinterpret_cast<unsigned short *>(b + i * stride + idx + 1) = 0x7777u;
+        }
+        store_pair<L27, S>(dn, idx, d2, false, 0u, 0u, (uint32_t)keep);
+        for (int i = 0; i < 27; i++) {
+            const S ea = (S)da[i], eb = (S)db[i];
+            const unsigned short w0 = keep == 1 ? *reinterpret_cast<const unsigned short *>(&ea) : 0x7777u;
+            const unsigned short w1 = keep == 2 ? *reinterpret_cast<const unsigned short *>(&eb) : 0x7777u;
+            if (*reinterpret_cast<unsigned short *>(b + i * stride + idx) != w0 ||
+                *reinterpret_cast<unsigned short *>(b + i * stride + idx + 1) != w1)
+                atomicOr(bad, 512);
+        }
+    }
 }
 
 int main() {
@@ -110,6 +139,7 @@ int main() {
     cudaFree(ha);
     cudaFree(ba);
     printf("pair vs scalar mismatch bits: force-free / FP16 stores %d, forced / BF16 stores %d "
-           "(1 moments, 2 velocity, 4 collision, 8 aneq, 16 Aq, 32 Bq, 64 Bn, 128 rounded stores)\n", h[0], h[1]);
+           "(1 moments, 2 velocity, 4 collision, 8 aneq, 16 Aq, 32 Bq, 64 Bn, 128 stochastic stores, "
+           "256 nearest stores, 512 one node of a pair)\n", h[0], h[1]);
     return (h[0] || h[1]) ? 1 : 0;
 }
