@@ -1,6 +1,8 @@
-// kernels for float population storage (see rr_inst.inc)
+// kernels for float population storage (see rr_inst.inc): all but the tile step and the batch
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #define RR_STORE float
 #define RR_OPS_NAME ops_f32
+#define RR_IMPL_NS impl_f32
+#define RR_PART 2
 #include "rr_inst.inc"

@@ -587,9 +587,15 @@ __device__ __forceinline__ void tile_node(const A &a, uint32_t row, int x, int y
 // and high half i1; one packed conversion rounds population i of both nodes,
 // the first node's bits in the low half of the random operand, the second's
 // in the high.
-template <class LT, typename S>
+template <class LT, typename S, bool PARTIAL = false>
 __device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, const F2 (&d)[LT::Q], bool sround,
                                            uint32_t sa, uint32_t sb, uint32_t keep = 3u) {
+    // keep: 3 both nodes, 0 neither; PARTIAL also 1 / 2 (one node: one more
+    // store instruction per population for the whole warp)
+    auto put = [&](S *p, typename PairWord<S>::W w) {
+        if constexpr (PARTIAL) put_word<S>(p, w, keep);
+        else if (keep != 0u) *reinterpret_cast<typename PairWord<S>::W *>(p) = w;
+    };
     if constexpr (std::is_same<S, __half>::value || std::is_same<S, __nv_bfloat16>::value) {
         if (sround) {
             uint32_t ra = sa, rb = sb;
@@ -598,21 +604,21 @@ __device__ __forceinline__ void store_pair(S *const *dst, uint32_t ia, const F2 
                 ra = ra * 1664525u + 1013904223u;
                 rb = rb * 1664525u + 1013904223u;
                 const uint32_t fa = ra ^ (ra >> 16), fb = rb ^ (rb >> 16);
-                put_word<S>(dst[i0] + ia, cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)), keep);
-                if constexpr (i1 < LT::Q)
-                    put_word<S>(dst[i1] + ia, cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)), keep);
+                put(dst[i0] + ia, cvt_sr2<S>(d[i0].hi(), d[i0].lo(), __byte_perm(fa, fb, 0x5410)));
+                if constexpr (i1 < LT::Q) put(dst[i1] + ia, cvt_sr2<S>(d[i1].hi(), d[i1].lo(), __byte_perm(fa, fb, 0x7632)));
             });
             return;
         }
     }
     static_for<LT::Q>([&](auto ic) {
         constexpr int i = decltype(ic)::value;
-        put_word<S>(dst[i] + ia, word_of<S>(d[i]), keep);
+        put(dst[i] + ia, word_of<S>(d[i]));
     });
 }
 
 // the DNS step of the node pair ia, ia + 1 from its post-stream populations
-// d: moments, the watchdog, the collision, the stores (of the nodes in keep)
+// d: moments, the watchdog, the collision, the stores (keep: 3 both nodes, 0
+// neither: the pair belongs to another item)
 template <class LT, typename S, bool FORCE>
 __device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, S *const *dst, double om1_, const double *Fv,
                                           int *status, bool sround, uint32_t keep) {
@@ -637,9 +643,8 @@ __device__ __forceinline__ void pair_core(F2 (&d)[LT::Q], uint32_t ia, S *const 
 // their missing element alone, wrapped periodically in x.  Every lane of the
 // warp must call this (the shuffles take all 32).  The pair is collided in
 // packed FP32 (pair_core), bit for bit the scalar node arithmetic.  xends:
-// the x = 0 and x = nx-1 nodes (x walls) belong to the x-face items; the lanes
-// holding them compute their pair (the wall node from wrapped values) and
-// store only the other node.
+// x walls, whose end pairs (0, 1) and (nx-2, nx-1) belong to the x-face items
+// (xend_pair); the lanes holding them only feed their neighbours' shuffles.
 template <class LT, typename S, bool FORCE, class A>
 __device__ __forceinline__ void pair_row(const A &a, uint32_t row, int x0, uint32_t lane, bool xends) {
     using W = typename PairWord<S>::W;
@@ -702,8 +707,50 @@ __device__ __forceinline__ void pair_row(const A &a, uint32_t row, int x0, uint3
         });
     }
     if (!active) return;
-    const uint32_t keep = !xends ? 3u : x == 0 ? 2u : x + 2 == nx ? 1u : 3u;
+    const uint32_t keep = xends && (x == 0 || x + 2 == nx) ? 0u : 3u;
     pair_core<LT, S, FORCE>(d, rbase + (uint32_t)x, a.dst, a.om1, a.F, a.status, g.sround != 0, keep);
+}
+
+// The end pair of a row off every y/z face with x walls, in an x-face item
+// (one row per lane): LO the pair (0, 1), else (nx-2, nx-1).  The words of
+// the pair from the upstream rows, the inner node's shifted element alone;
+// the wall node's entering populations bounce back with that face's closure
+// in scalar FP32 (wall_face, as the node alone gets it); then both nodes
+// collide as a packed pair and store whole words.
+template <class LT, typename S, bool FORCE, bool LO, class A>
+__device__ __forceinline__ void xend_pair(const A &a, uint32_t row) {
+    using W = typename PairWord<S>::W;
+    const Geom &g = a.g;
+    const int nx = g.nx;
+    const uint32_t rbase = row * (uint32_t)nx;
+    const int x = LO ? 0 : nx - 2;
+    const uint32_t idx = rbase + (uint32_t)x;
+    W v[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        constexpr int cx = LT::cx(i);
+        const S *up = a.src[i] + (rbase + (uint32_t)cx);
+        W w = ld_word<S>(up + x);
+        // the wall node's entering element (0 here) is replaced below
+        if constexpr (cx == 1) w = join_word<S>(LO ? W(0) : elem_hi<S>(up + (x - 1)), w);
+        if constexpr (cx == -1) w = join_word<S>(w, LO ? elem_lo<S>(up + (x + 2)) : W(0));
+        v[i] = w;
+    });
+    float t[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        t[i] = LO ? word_f2<S>(v[i]).lo() : word_f2<S>(v[i]).hi();
+    });
+    const float Fx = float(a.F[0]), Fy = float(a.F[1]), Fz = float(a.F[2]);
+    if constexpr (LO) wall_face<LT, S, float, FORCE, 0>(a.fin, g, idx, t, Fx, Fy, Fz);
+    else wall_face<LT, S, float, FORCE, 1>(a.fin, g, idx + 1u, t, Fx, Fy, Fz);
+    F2 d[LT::Q];
+    static_for<LT::Q>([&](auto ic) {
+        constexpr int i = decltype(ic)::value;
+        const F2 w = word_f2<S>(v[i]);
+        d[i] = LO ? F2(t[i], w.hi()) : F2(w.lo(), t[i]);
+    });
+    pair_core<LT, S, FORCE>(d, idx, a.dst, a.om1, a.F, a.status, g.sround != 0, 3u);
 }
 
 // A row item of the aligned pair layout, a 64-node segment of one row: false
@@ -816,6 +863,15 @@ __device__ __forceinline__ void tile_item(const A &a, uint32_t item, uint32_t la
     int x, y, z;
     bool fast;
     if (!tile_decode(a, item, lane, row, x, y, z, fast)) return;
+    if constexpr (PAIRABLE) {
+        // pair layout: an x-face node of a row off every y/z face takes its
+        // end pair
+        if (a.pairs && y >= 1 && y <= a.g.ny - 2 && z >= 1 && z <= a.g.nz - 2) {
+            if (x == 0) xend_pair<LT, S, FORCE, true>(a, row);
+            else xend_pair<LT, S, FORCE, false>(a, row);
+            return;
+        }
+    }
     tile_node<LT, S, FORCE, MODE, FIELD, BGK>(a, row, x, y, z, fast);
 }
 

@@ -1,5 +1,7 @@
-"""Builds librrlbm.so in-tree with nvcc for sm_103a (one -gencode, one
-translation unit per population storage type, compiled in parallel)."""
+"""Builds librrlbm.so in-tree with nvcc for sm_103a (one -gencode; the
+kernels of each population storage type in one translation unit, or two for
+the 16/32-bit types whose tile step and batch carry the packed-pair paths;
+all compiled in parallel)."""
 import os
 import subprocess
 import sys
@@ -14,8 +16,10 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-I", INCLUDE]
-SOURCES = ["rr_inst_f64.cu", "rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.cu",
-           "rr_aux.cu", "rr_api.cu", "rr_batch.cu", "rr_noalloc.cu"]
+# the longest compiles first
+SOURCES = ["rr_inst_f16_tile.cu", "rr_inst_bf16_tile.cu", "rr_inst_f32_tile.cu", "rr_inst_f64.cu",
+           "rr_inst_f32.cu", "rr_inst_f16.cu", "rr_inst_bf16.cu", "rr_aux.cu", "rr_api.cu", "rr_batch.cu",
+           "rr_noalloc.cu"]
 HEADERS = ["rr_lattice.cuh", "rr_node.cuh", "rr_node27.cuh", "rr_kernels.cuh", "rr_les.cuh", "rr_dispatch.h",
            "rr_aux.h", "rr_inst.inc", "rr_internal.h", "rr_stage.cuh", "rr_fdbc.cuh", "rr_pair.cuh"]
 
@@ -43,7 +47,7 @@ def build(verbose=False, force=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         return cmd, r
 
-    with ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
+    with ThreadPoolExecutor(max_workers=min(16, max(1, len(jobs)))) as ex:
         for cmd, r in ex.map(run, jobs):
             if verbose or r.returncode != 0:
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

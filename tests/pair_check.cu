@@ -106,7 +106,7 @@ __global__ void check_store(int *bad, int n, S *a, S *b) {
             *reinterpret_cast<unsigned short *>(b + i * stride + idx) = 0x7777u;
             *reinterpret_cast<unsigned short *>(b + i * stride + idx + 1) = 0x7777u;
         }
-        store_pair<L27, S>(dn, idx, d2, false, 0u, 0u, (uint32_t)keep);
+        store_pair<L27, S, true>(dn, idx, d2, false, 0u, 0u, (uint32_t)keep);
         for (int i = 0; i < 27; i++) {
             const S ea = (S)da[i], eb = (S)db[i];
             const unsigned short w0 = keep == 1 ? *reinterpret_cast<const unsigned short *>(&ea) : 0x7777u;
