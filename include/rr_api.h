@@ -134,7 +134,10 @@ rr_status rr_destroy(rr_solver *s);
  * p->order) and the macroscopic fields the first collision uses
  * (init_arrays, initial.cu:268-326, and the CONTINUE_STEP restart,
  * initial.cu:189-265).  f may be NULL: the second-order equilibrium of
- * (rho, u) is used (Cavity/initial.f90:3-34).  Resets the step counter. */
+ * (rho, u) is used (Cavity/initial.f90:3-34).  Resets the step counter.
+ * With RR_HOST the call returns once the host arrays are copied (the caller
+ * may reuse them); the upload and first collision run on, in order on the
+ * solver's stream. */
 rr_status rr_init_state(rr_solver *s, const double *f, const double *rho, const double *ux,
                         const double *uy, const double *uz, int where);
 
