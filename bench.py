@@ -393,8 +393,8 @@ def run_gpu(args, rank, world, local_rank):
         # the reference's CPU programs are serial: the like-for-like line
         line["cpu_baseline_1core"] = cpu_baseline(args.workload, args.cpu_seconds / 2, cores=1)
     if world == 1 and args.batch_steps > 0:
+        # the batch section's own timed region keeps its own launch count
         line["batch"] = run_batch(args)
-        line["gpu_launches"] += line["batch"].pop("launches")
     if world == 1 and args.serve_requests > 0:
         line["serving"] = run_serve(args)
     print(json.dumps(line), flush=True)
